@@ -1,0 +1,969 @@
+// Host orchestration and C ABI of libFourierConvolutionCUDALib.so (GB300).
+//
+// Replaces the reference's host layer (src/convolution3Dfft.cu:216-603 and
+// src/standardCUDAfunctions.cu:13-71).  Differences by design:
+//   * no exit() and no exception crosses the C ABI: failures set a
+//     thread-local status/message (fc_last_status / fc_last_error);
+//   * one context per device holds a stream, a grow-only workspace, device
+//     buffers for the host entry points and the twiddle tables per length;
+//     calls on the same device serialise on the context's mutex;
+//   * the FFT is this library's own (fc_fft.cuh); the spectrum product and the
+//     kernel padding/shift are fused into the passes (fc_kernels.cu).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/convolution3Dfft.h"
+#include "fc_internal.h"
+
+namespace fc {
+
+// ------------------------------------------------------------------ status
+static thread_local int t_status = FC_OK;
+static thread_local std::string t_error;
+static thread_local int t_launches = 0;
+
+struct FcError {
+  int code;
+  std::string msg;
+};
+
+static void set_status(int code, const std::string& msg) {
+  t_status = code;
+  t_error = msg;
+}
+static void clear_status() {
+  t_status = FC_OK;
+  t_error.clear();
+  t_launches = 0;
+}
+
+#define FC_THROW(code, msg)      \
+  do {                           \
+    throw FcError{(code), (msg)}; \
+  } while (0)
+
+static void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    const int code = (e == cudaErrorMemoryAllocation) ? FC_ERR_NOMEM : FC_ERR_CUDA;
+    FC_THROW(code, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+// ------------------------------------------------------------------ radix plans
+static const int kMaxAxis = 4096;
+
+// Factor n into stages: powers of two as evenly sized radix-16/8/4/2 stages,
+// then 3, 5, 7, 11, 13 butterflies, then any remaining prime as a generic stage.
+static int plan_radices(int n, int* out, int maxs) {
+  if (n < 1) return -1;
+  std::vector<int> r;
+  int m = n, a = 0;
+  while ((m & 1) == 0) {
+    m >>= 1;
+    ++a;
+  }
+  if (a > 0) {
+    const int s = (a + 3) / 4;
+    int rem = a;
+    for (int i = 0; i < s; ++i) {
+      const int e = (rem + (s - i) - 1) / (s - i);  // ceil(rem / stages left)
+      r.push_back(1 << e);
+      rem -= e;
+    }
+  }
+  const int small[] = {3, 5, 7, 11, 13};
+  for (int p : small) {
+    while (m % p == 0) {
+      r.push_back(p);
+      m /= p;
+    }
+  }
+  for (int p = 17; (long long)p * p <= m; p += 2) {
+    while (m % p == 0) {
+      r.push_back(p);
+      m /= p;
+    }
+  }
+  if (m > 1) r.push_back(m);
+  if (r.empty()) r.push_back(1);  // n == 1: identity stage handled as radix 1 -> generic
+  if ((int)r.size() > maxs) return -1;
+  // larger radices first: fewer twiddle multiplies in the early stages
+  for (size_t i = 0; i < r.size(); ++i) out[i] = r[i];
+  return (int)r.size();
+}
+
+// ------------------------------------------------------------------ device context
+struct DevCtx {
+  int dev = -1;
+  std::mutex mu;
+  cudaStream_t stream = nullptr;
+  void* ws = nullptr;
+  size_t ws_cap = 0;
+  float* d_img = nullptr;
+  size_t img_cap = 0;
+  float* d_ker = nullptr;
+  size_t ker_cap = 0;
+  std::map<int, float2*> twiddles;  // per transform length
+};
+
+static std::mutex g_ctx_mu;
+static std::map<int, std::unique_ptr<DevCtx>> g_ctx;
+static int g_shift_compat = -1;  // -1: not yet read from the environment
+
+static bool shift_compat_default() {
+  if (g_shift_compat < 0) {
+    const char* e = std::getenv("FC_SHIFT_COMPAT");
+    g_shift_compat = (e && std::atoi(e) != 0) ? 1 : 0;
+  }
+  return g_shift_compat == 1;
+}
+
+static int current_device() {
+  int d = 0;
+  cuda_check(cudaGetDevice(&d), "cudaGetDevice");
+  return d;
+}
+
+static DevCtx& ctx_for(int dev) {
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  auto it = g_ctx.find(dev);
+  if (it != g_ctx.end()) return *it->second;
+  auto c = std::make_unique<DevCtx>();
+  c->dev = dev;
+  DevCtx& ref = *c;
+  g_ctx[dev] = std::move(c);
+  return ref;
+}
+
+static cudaStream_t ctx_stream(DevCtx& c) {
+  if (!c.stream) cuda_check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  return c.stream;
+}
+
+static void grow(void** p, size_t* cap, size_t need, const char* what) {
+  if (need <= *cap) return;
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+  }
+  cuda_check(cudaMalloc(p, need), what);
+  *cap = need;
+}
+
+// twiddle table W[k] = exp(-2 pi i k / n), double precision rounded once
+static const float2* twiddles_for(DevCtx& c, int n) {
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  auto it = c.twiddles.find(n);
+  if (it != c.twiddles.end()) return it->second;
+  std::vector<float2> h(n);
+  for (int k = 0; k < n; ++k) {
+    const double ang = -2.0 * M_PI * (double)k / (double)n;
+    h[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+  }
+  float2* d = nullptr;
+  cuda_check(cudaMalloc(&d, sizeof(float2) * n), "cudaMalloc(twiddles)");
+  cuda_check(cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice), "cudaMemcpy(twiddles)");
+  c.twiddles[n] = d;
+  return d;
+}
+
+static FcAxis make_axis(DevCtx& c, int n) {
+  FcAxis ax;
+  std::memset(&ax, 0, sizeof(ax));
+  ax.n = n;
+  int r[FC_MAX_STAGES];
+  const int s = plan_radices(n, r, FC_MAX_STAGES);
+  if (s < 0) FC_THROW(FC_ERR_UNSUPPORTED, "no radix plan for length " + std::to_string(n));
+  ax.nst = (n == 1) ? 0 : s;
+  for (int i = 0; i < s; ++i) ax.radix[i] = r[i];
+  ax.W = twiddles_for(c, n);
+  return ax;
+}
+
+// ------------------------------------------------------------------ geometry
+static int ilog2_floor(long long v) {
+  int l = 0;
+  while ((2LL << l) <= v) ++l;
+  return l;
+}
+
+static Tiles choose_tiles(const Geom& g) {
+  Tiles t;
+  t.threads = 256;
+  // x passes: about 2048 complex values per CTA (two real rows per line)
+  long long P = std::max(1LL, 2048LL / std::max(1, g.nx));
+  P = std::min(P, 64LL);
+  t.x_pairs_log2 = ilog2_floor(P);
+  // y passes: about 4096 complex values per tile (64 KiB of shared memory for 2 buffers)
+  long long By = std::max(1LL, std::min(32LL, 4096LL / std::max(1, g.ny)));
+  t.y_cols_log2 = ilog2_floor(By);
+  // z pass holds image and kernel columns: about 2048 columns x rows
+  long long Bz = std::max(1LL, std::min(32LL, 2048LL / std::max(1, g.nz)));
+  t.z_cols_log2 = ilog2_floor(Bz);
+  return t;
+}
+
+static long long spectrum_pitch(int nxh) {
+  if (nxh >= 64) return ((long long)nxh + 15) / 16 * 16;
+  return ((long long)nxh + 1) / 2 * 2;
+}
+
+static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+static void validate_dims(int nx, int ny, int nz) {
+  if (nx < 1 || ny < 1 || nz < 1) FC_THROW(FC_ERR_ARG, "image dimensions must be positive");
+  if (nx > kMaxAxis || ny > kMaxAxis || nz > kMaxAxis)
+    FC_THROW(FC_ERR_UNSUPPORTED, "axis longer than " + std::to_string(kMaxAxis) + " is not supported by this build");
+}
+
+static Geom make_geom(int nx, int ny, int nz, int kx, int ky, int kz, bool dense) {
+  validate_dims(nx, ny, nz);
+  Geom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.nxh = nx / 2 + 1;
+  g.pitch = spectrum_pitch(g.nxh);
+  g.kbox = !dense;
+  if (dense) {
+    g.kx = nx;
+    g.ky = ny;
+    g.kz = nz;
+    g.kplanes = nz;
+    g.krows = ny;
+  } else {
+    if (kx < 1 || ky < 1 || kz < 1) FC_THROW(FC_ERR_ARG, "kernel dimensions must be positive");
+    if (kx > nx || ky > ny || kz > nz) FC_THROW(FC_ERR_ARG, "kernel larger than the image along an axis");
+    g.kx = kx;
+    g.ky = ky;
+    g.kz = kz;
+    g.kplanes = kz;
+    g.krows = ky;
+  }
+  return g;
+}
+
+// Plain convolution workspace: S (image spectrum), KX (kernel x-spectrum rows,
+// box mode only), KXY (kernel xy-spectrum planes), dense (materialised kernel
+// for the reference-arithmetic placement).
+static Layout conv_layout(const Geom& g, bool compat_dense) {
+  Layout L;
+  size_t o = 0;
+  const size_t row = (size_t)g.pitch * sizeof(float2);
+  L.off_S = o;
+  o = align256(o + row * g.ny * g.nz);
+  L.off_KX = o;
+  if (g.kbox) o = align256(o + row * g.krows * g.kplanes);
+  L.off_KXY = o;
+  o = align256(o + row * g.ny * g.kplanes);
+  L.off_dense = o;
+  if (compat_dense) o = align256(o + sizeof(float) * (size_t)g.N());
+  L.off_aux = o;
+  L.total = o;
+  return L;
+}
+
+// ------------------------------------------------------------------ profiling
+struct ProfRec {
+  std::string name;
+  cudaEvent_t a, b;
+  double bytes;
+};
+static std::mutex g_prof_mu;
+static bool g_prof_on = false;
+static std::vector<ProfRec> g_prof;
+
+struct PassScope {
+  bool on;
+  cudaEvent_t a = nullptr, b = nullptr;
+  const char* name;
+  double bytes;
+  cudaStream_t st;
+  PassScope(const char* nm, double by, cudaStream_t s) : on(g_prof_on), name(nm), bytes(by), st(s) {
+    if (on) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, st);
+    }
+  }
+  ~PassScope() {
+    if (on) {
+      cudaEventRecord(b, st);
+      std::lock_guard<std::mutex> lk(g_prof_mu);
+      g_prof.push_back(ProfRec{name, a, b, bytes});
+    }
+  }
+};
+
+#define FC_PASS(name, bytes, st, call)                \
+  do {                                                \
+    PassScope _ps((name), (double)(bytes), (st));     \
+    cuda_check((call), name);                         \
+    ++t_launches;                                     \
+  } while (0)
+
+// ------------------------------------------------------------------ pass chains
+struct Axes {
+  FcAxis x, y, z;
+};
+
+static Axes axes_for(DevCtx& c, const Geom& g) {
+  Axes a;
+  a.x = make_axis(c, g.nx);
+  a.y = make_axis(c, g.ny);
+  a.z = make_axis(c, g.nz);
+  return a;
+}
+
+// kernel spectrum KXY from taps (box) or a dense N-float kernel
+static void enqueue_kernel_spectrum(const Geom& g, const Axes& a, const Tiles& t, const float* d_kernel, char* ws,
+                                    const Layout& L, cudaStream_t st) {
+  float2* KX = (float2*)(ws + L.off_KX);
+  float2* KXY = (float2*)(ws + L.off_KXY);
+  const double row = (double)g.pitch * 8.0;
+  if (g.kbox) {
+    const long long rows = (long long)g.kplanes * g.krows;
+    FC_PASS("kernel_x_r2c", 4.0 * g.kx * rows + 8.0 * g.nxh * rows, st,
+            launch_x_r2c_box(d_kernel, g.kx, g.kx / 2, KX, g.pitch, rows, a.x, t, st));
+    FC_PASS("kernel_y_fwd", 8.0 * g.nxh * (rows + (double)g.ny * g.kplanes), st,
+            launch_cols_kx(KX, g.pitch, g.krows, g.ky / 2, KXY, g.nxh, g.kplanes, a.y, t.y_cols_log2, t.threads, st));
+  } else {
+    const long long rows = (long long)g.ny * g.nz;
+    FC_PASS("kernel_x_r2c", 4.0 * g.nx * rows + 8.0 * g.nxh * rows, st,
+            launch_x_r2c_dense(d_kernel, g.nx, KXY, g.pitch, rows, a.x, t, st));
+    FC_PASS("kernel_y_fwd", 16.0 * g.nxh * rows, st,
+            launch_cols(KXY, KXY, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2,
+                        t.threads, st));
+  }
+  (void)row;
+}
+
+// forward x and y passes of a real volume into spectrum S
+static void enqueue_xy_fwd(const Geom& g, const Axes& a, const Tiles& t, const float* d_in, float2* S,
+                           cudaStream_t st, const char* xname, const char* yname) {
+  const long long rows = (long long)g.ny * g.nz;
+  FC_PASS(xname, 4.0 * g.N() + 8.0 * g.nxh * rows, st, launch_x_r2c_dense(d_in, g.nx, S, g.pitch, rows, a.x, t, st));
+  FC_PASS(yname, 16.0 * g.nxh * rows, st,
+          launch_cols(S, S, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2, t.threads,
+                      st));
+}
+
+static void enqueue_yx_inv(const Geom& g, const Axes& a, const Tiles& t, float2* S, float* d_out, cudaStream_t st,
+                           const char* yname, const char* xname) {
+  const long long rows = (long long)g.ny * g.nz;
+  FC_PASS(yname, 16.0 * g.nxh * rows, st,
+          launch_cols(S, S, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, true, a.y, t.y_cols_log2, t.threads,
+                      st));
+  FC_PASS(xname, 4.0 * g.N() + 8.0 * g.nxh * rows, st, launch_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
+}
+
+
+// The geometry the passes run on: the reference-arithmetic placement is
+// materialised into a dense buffer and then treated as a dense kernel.
+static Geom effective_geom(const Geom& g, bool compat) {
+  return (compat && g.kbox) ? make_geom(g.nx, g.ny, g.nz, 0, 0, 0, true) : g;
+}
+static Layout plain_layout(const Geom& g, bool compat) { return conv_layout(effective_geom(g, compat), compat && g.kbox); }
+
+// Enqueue a full convolution.  d_kernel: taps (box) or dense N floats.
+static void enqueue_conv(DevCtx& c, const Geom& g0, const float* d_image, float* d_out, const float* d_kernel,
+                         bool compat, char* ws, size_t ws_bytes, cudaStream_t st) {
+  const Geom g = effective_geom(g0, compat);
+  const Layout L = conv_layout(g, compat && g0.kbox);
+  if (ws_bytes < L.total) FC_THROW(FC_ERR_NOMEM, "workspace too small");
+  const float* ksrc = d_kernel;
+  if (compat && g0.kbox) {
+    float* dense = (float*)(ws + L.off_dense);
+    cuda_check(cudaMemsetAsync(dense, 0, sizeof(float) * (size_t)g.N(), st), "cudaMemsetAsync");
+    FC_PASS("kernel_pad_shift_compat", 8.0 * g0.kx * g0.ky * g0.kz, st,
+            launch_pad_shift(d_kernel, g0.kx, g0.ky, g0.kz, g0.nx, g0.ny, g0.nz, true, dense, st));
+    ksrc = dense;
+  }
+  const Tiles t = choose_tiles(g);
+  const Axes a = axes_for(c, g);
+  float2* S = (float2*)(ws + L.off_S);
+  enqueue_kernel_spectrum(g, a, t, ksrc, ws, L, st);
+  enqueue_xy_fwd(g, a, t, d_image, S, st, "image_x_r2c", "image_y_fwd");
+  const double mcy = 8.0 * g.nxh * (double)g.ny * g.nz;
+  FC_PASS("zconv", 2.0 * mcy + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
+          launch_zconv(S, (const float2*)(ws + L.off_KXY), g.pitch, g.ny, g.nxh, g.kplanes, g.kbox ? g.kz / 2 : 0,
+                       1.0f / (float)g.N(), false, a.z, t.z_cols_log2, t.threads, st));
+  enqueue_yx_inv(g, a, t, S, d_out, st, "image_y_inv", "image_x_c2r");
+}
+
+// ------------------------------------------------------------------ adjoint
+// Workspace: SG (gradient spectrum), SX (image spectrum), KX/KXY (kernel
+// spectrum), GK (kernel-gradient spectrum, kernel planes only) and GKR (its
+// real rows before the crop).
+struct AdjLayout {
+  size_t off_SG, off_SX, off_KX, off_KXY, off_GK, off_GKR, total;
+};
+static AdjLayout adj_layout(const Geom& g) {
+  AdjLayout L;
+  const size_t row = (size_t)g.pitch * sizeof(float2);
+  size_t o = 0;
+  L.off_SG = o;
+  o = align256(o + row * g.ny * g.nz);
+  L.off_SX = o;
+  o = align256(o + row * g.ny * g.nz);
+  L.off_KX = o;
+  if (g.kbox) o = align256(o + row * g.krows * g.kplanes);
+  L.off_KXY = o;
+  o = align256(o + row * g.ny * g.kplanes);
+  L.off_GK = o;
+  o = align256(o + row * g.ny * g.kplanes);
+  L.off_GKR = o;
+  o = align256(o + sizeof(float) * (size_t)g.nx * g.ny * g.kplanes);
+  L.total = o;
+  return L;
+}
+
+static void enqueue_adjoint(DevCtx& c, const Geom& g, const float* d_x, const float* d_k, const float* d_g,
+                            float* d_gx, float* d_gk, char* ws, size_t ws_bytes, cudaStream_t st) {
+  const AdjLayout L = adj_layout(g);
+  if (ws_bytes < L.total) FC_THROW(FC_ERR_NOMEM, "workspace too small");
+  const Tiles t = choose_tiles(g);
+  const Axes a = axes_for(c, g);
+  float2* SG = (float2*)(ws + L.off_SG);
+  float2* SX = (float2*)(ws + L.off_SX);
+  float2* GK = (float2*)(ws + L.off_GK);
+  float* GKR = (float*)(ws + L.off_GKR);
+  const float scale = 1.0f / (float)g.N();
+  const int hz = g.kbox ? g.kz / 2 : 0;
+  enqueue_xy_fwd(g, a, t, d_g, SG, st, "grad_x_r2c", "grad_y_fwd");
+  if (d_gk) {
+    enqueue_xy_fwd(g, a, t, d_x, SX, st, "image_x_r2c", "image_y_fwd");
+    FC_PASS("zcorr_crop", 16.0 * g.nxh * (double)g.ny * g.nz + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
+            launch_zcorr_crop(SX, SG, GK, g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, a.z, t.z_cols_log2, t.threads,
+                              st));
+  }
+  if (d_gx) {
+    Layout kl;
+    kl.off_KX = L.off_KX;
+    kl.off_KXY = L.off_KXY;
+    enqueue_kernel_spectrum(g, a, t, d_k, ws, kl, st);
+    FC_PASS("zconv_conj", 16.0 * g.nxh * (double)g.ny * g.nz + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
+            launch_zconv(SG, (const float2*)(ws + L.off_KXY), g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, true, a.z,
+                         t.z_cols_log2, t.threads, st));
+    enqueue_yx_inv(g, a, t, SG, d_gx, st, "grad_image_y_inv", "grad_image_x_c2r");
+  }
+  if (d_gk) {
+    const long long rows = (long long)g.ny * g.kplanes;
+    FC_PASS("grad_kernel_y_inv", 16.0 * g.nxh * rows, st,
+            launch_cols(GK, GK, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.kplanes, true, a.y, t.y_cols_log2,
+                        t.threads, st));
+    float* dst = g.kbox ? GKR : d_gk;
+    FC_PASS("grad_kernel_x_c2r", 8.0 * g.nxh * rows + 4.0 * g.nx * rows, st,
+            launch_x_c2r(GK, g.pitch, dst, g.nx, rows, a.x, t, st));
+    if (g.kbox)
+      FC_PASS("grad_kernel_crop", 8.0 * g.kx * g.ky * g.kz, st,
+              launch_crop_kernel(GKR, g.nx, g.ny, g.nx, g.kx, g.ky, g.kz, d_gk, st));
+  }
+}
+
+// ------------------------------------------------------------------ raw transforms
+static size_t fft_ws_bytes(const Geom& g) { return align256((size_t)g.pitch * sizeof(float2) * g.ny * g.nz); }
+
+static void enqueue_rfft3d(DevCtx& c, const Geom& g, const float* d_in, float* d_spec, char* ws, size_t wsb,
+                           cudaStream_t st) {
+  if (wsb < fft_ws_bytes(g)) FC_THROW(FC_ERR_NOMEM, "workspace too small");
+  const Tiles t = choose_tiles(g);
+  const Axes a = axes_for(c, g);
+  float2* S = (float2*)ws;
+  enqueue_xy_fwd(g, a, t, d_in, S, st, "fft_x_r2c", "fft_y_fwd");
+  // z pass as a column pass over planes of constant y; the result is written
+  // into the caller's dense layout (pitch nxh) by a final strided z pass
+  FC_PASS("fft_z_fwd", 16.0 * g.nxh * (double)g.ny * g.nz, st,
+          launch_cols(S, S, g.pitch, (long long)g.ny * g.pitch, g.nxh, g.ny, false, a.z, t.z_cols_log2, t.threads,
+                      st));
+  cuda_check(cudaMemcpy2DAsync(d_spec, sizeof(float2) * g.nxh, S, sizeof(float2) * g.pitch, sizeof(float2) * g.nxh,
+                               (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, st),
+             "cudaMemcpy2DAsync");
+}
+
+static void enqueue_irfft3d(DevCtx& c, const Geom& g, const float* d_spec, float* d_out, char* ws, size_t wsb,
+                            cudaStream_t st) {
+  if (wsb < fft_ws_bytes(g)) FC_THROW(FC_ERR_NOMEM, "workspace too small");
+  const Tiles t = choose_tiles(g);
+  const Axes a = axes_for(c, g);
+  float2* S = (float2*)ws;
+  cuda_check(cudaMemcpy2DAsync(S, sizeof(float2) * g.pitch, d_spec, sizeof(float2) * g.nxh, sizeof(float2) * g.nxh,
+                               (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, st),
+             "cudaMemcpy2DAsync");
+  FC_PASS("fft_z_inv", 16.0 * g.nxh * (double)g.ny * g.nz, st,
+          launch_cols(S, S, g.pitch, (long long)g.ny * g.pitch, g.nxh, g.ny, true, a.z, t.z_cols_log2, t.threads, st));
+  enqueue_yx_inv(g, a, t, S, d_out, st, "fft_y_inv", "fft_x_c2r");
+}
+
+// ------------------------------------------------------------------ host entry points
+static void set_device(int dev) {
+  int n = 0;
+  cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+  if (dev < 0 || dev >= n) FC_THROW(FC_ERR_ARG, "invalid device index " + std::to_string(dev));
+  cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+}
+
+// Host-pointer convolution used by the three reference-compatible entry points.
+static void host_conv(const float* im, float* out, int nx, int ny, int nz, const float* kernel, int kx, int ky,
+                      int kz, bool dense, int dev) {
+  if (!im || !out || !kernel) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+  const Geom g = make_geom(nx, ny, nz, kx, ky, kz, dense);
+  set_device(dev);
+  const bool compat = shift_compat_default() && g.kbox;
+  DevCtx& c = ctx_for(dev);
+  std::lock_guard<std::mutex> lk(c.mu);
+  cudaStream_t st = ctx_stream(c);
+  const size_t wsb = plain_layout(g, compat).total;
+  const size_t nimg = sizeof(float) * (size_t)g.N();
+  const size_t nker = sizeof(float) * (dense ? (size_t)g.N() : (size_t)kx * ky * kz);
+  grow(&c.ws, &c.ws_cap, wsb, "cudaMalloc(workspace)");
+  grow((void**)&c.d_img, &c.img_cap, nimg, "cudaMalloc(image)");
+  grow((void**)&c.d_ker, &c.ker_cap, nker, "cudaMalloc(kernel)");
+  cuda_check(cudaMemcpyAsync(c.d_ker, kernel, nker, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(kernel H2D)");
+  cuda_check(cudaMemcpyAsync(c.d_img, im, nimg, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(image H2D)");
+  enqueue_conv(c, g, c.d_img, c.d_img, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
+  cuda_check(cudaMemcpyAsync(out, c.d_img, nimg, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync(result D2H)");
+  cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+}
+
+template <class F>
+static int guarded(F&& f) {
+  try {
+    f();
+    return FC_OK;
+  } catch (const FcError& e) {
+    set_status(e.code, e.msg);
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_status(FC_ERR_NOMEM, "host allocation failed");
+    return FC_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    set_status(FC_ERR_CUDA, e.what());
+    return FC_ERR_CUDA;
+  } catch (...) {
+    set_status(FC_ERR_CUDA, "unknown failure");
+    return FC_ERR_CUDA;
+  }
+}
+
+static void* resolve_ws(DevCtx& c, void* d_ws, size_t* bytes, size_t need) {
+  if (d_ws) {
+    if (*bytes < need) FC_THROW(FC_ERR_NOMEM, "workspace smaller than required");
+    if (((uintptr_t)d_ws & 255) != 0) FC_THROW(FC_ERR_ARG, "workspace must be 256-byte aligned");
+    return d_ws;
+  }
+  grow(&c.ws, &c.ws_cap, need, "cudaMalloc(workspace)");
+  *bytes = c.ws_cap;
+  return c.ws;
+}
+
+static void dims3(const int* d, int* a, int* b, int* cc) {
+  if (!d) FC_THROW(FC_ERR_ARG, "NULL dimension array");
+  *a = d[0];
+  *b = d[1];
+  *cc = d[2];
+}
+
+}  // namespace fc
+
+using namespace fc;
+
+// ====================================================================== C ABI
+extern "C" {
+
+int fc_last_status(void) { return t_status; }
+const char* fc_last_error(void) { return t_error.c_str(); }
+void fc_free_result(imageType* p) { delete[] p; }
+void fc_set_shift_compat(int on) { g_shift_compat = on ? 1 : 0; }
+const char* fc_version(void) { return "fc-gb300 0.1.0 (sm_103a)"; }
+int fc_launch_count(void) { return t_launches; }
+
+int fc_plan_radices(int n, int* radices, int max_stages) {
+  if (!radices || max_stages < 1) return -1;
+  return plan_radices(n, radices, max_stages);
+}
+
+imageType* convolution3DfftCUDA_test(imageType* im, int* imDim, imageType* kernel, int devCUDA) {
+  clear_status();
+  imageType* out = nullptr;
+  const int rc = guarded([&] {
+    int d0, d1, d2;
+    dims3(imDim, &d0, &d1, &d2);
+    if (d0 < 1 || d1 < 1 || d2 < 1) FC_THROW(FC_ERR_ARG, "image dimensions must be positive");
+    out = new imageType[(size_t)d0 * d1 * d2];
+    host_conv(im, out, d2, d1, d0, kernel, 0, 0, 0, true, devCUDA);
+  });
+  if (rc != FC_OK) {
+    delete[] out;
+    return nullptr;
+  }
+  return out;
+}
+
+imageType* convolution3DfftCUDA(imageType* im, int* imDim, imageType* kernel, int* kernelDim, int devCUDA) {
+  clear_status();
+  imageType* out = nullptr;
+  const int rc = guarded([&] {
+    int d0, d1, d2, k0, k1, k2;
+    dims3(imDim, &d0, &d1, &d2);
+    dims3(kernelDim, &k0, &k1, &k2);
+    if (d0 < 1 || d1 < 1 || d2 < 1) FC_THROW(FC_ERR_ARG, "image dimensions must be positive");
+    out = new imageType[(size_t)d0 * d1 * d2];
+    // dims are slowest-first here (index 2 fastest): x = d2, y = d1, z = d0
+    host_conv(im, out, d2, d1, d0, kernel, k2, k1, k0, false, devCUDA);
+  });
+  if (rc != FC_OK) {
+    delete[] out;
+    return nullptr;
+  }
+  return out;
+}
+
+void convolution3DfftCUDAInPlace(imageType* im, int* imDim, imageType* kernel, int* kernelDim, int devCUDA) {
+  clear_status();
+  guarded([&] {
+    int nx, ny, nz, kx, ky, kz;
+    dims3(imDim, &nx, &ny, &nz);
+    dims3(kernelDim, &kx, &ky, &kz);
+    host_conv(im, im, nx, ny, nz, kernel, kx, ky, kz, false, devCUDA);
+  });
+}
+
+int getNumDevicesCUDA(void) {
+  clear_status();
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    set_status(FC_ERR_CUDA, "cudaGetDeviceCount failed");
+    return 0;
+  }
+  return n;
+}
+
+static int cc_attr(int dev, cudaDeviceAttr which) {
+  int v = -1;
+  if (cudaDeviceGetAttribute(&v, which, dev) != cudaSuccess) {
+    cudaGetLastError();
+    set_status(FC_ERR_CUDA, "cudaDeviceGetAttribute failed");
+    return -1;
+  }
+  return v;
+}
+
+int getCUDAcomputeCapabilityMajorVersion(int devCUDA) {
+  clear_status();
+  return cc_attr(devCUDA, cudaDevAttrComputeCapabilityMajor);
+}
+
+int getCUDAcomputeCapabilityMinorVersion(int devCUDA) {
+  clear_status();
+  return cc_attr(devCUDA, cudaDevAttrComputeCapabilityMinor);
+}
+
+int selectDeviceWithHighestComputeCapability(void) {
+  clear_status();
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    set_status(FC_ERR_CUDA, "cudaGetDeviceCount failed");
+    return -1;
+  }
+  int best = -1, best_cc = 0;
+  for (int d = 0; d < n; ++d) {
+    const int ma = cc_attr(d, cudaDevAttrComputeCapabilityMajor);
+    const int mi = cc_attr(d, cudaDevAttrComputeCapabilityMinor);
+    if (ma < 0 || mi < 0) continue;
+    const int meta = 10 * ma + mi;  // same ordering as src/standardCUDAfunctions.cu:25
+    if (meta > best_cc) {
+      best_cc = meta;
+      best = d;
+    }
+  }
+  return best;
+}
+
+void getNameDeviceCUDA(int devCUDA, char* name) {
+  clear_status();
+  if (!name) {
+    set_status(FC_ERR_ARG, "NULL name buffer");
+    return;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, devCUDA) != cudaSuccess) {
+    cudaGetLastError();
+    std::memset(name, 0, 256);
+    set_status(FC_ERR_CUDA, "cudaGetDeviceProperties failed");
+    return;
+  }
+  std::memcpy(name, prop.name, 256);
+}
+
+long long int getMemDeviceCUDA(int devCUDA) {
+  clear_status();
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, devCUDA) != cudaSuccess) {
+    cudaGetLastError();
+    set_status(FC_ERR_CUDA, "cudaGetDeviceProperties failed");
+    return 0;
+  }
+  return (long long int)prop.totalGlobalMem;
+}
+
+int cuda_version(void) { return CUDART_VERSION; }
+
+int gpu_mem_needed_mb(int* shape, int len) {
+  clear_status();
+  long long mb = -1;
+  guarded([&] {
+    if (!shape || len < 1 || len > 3) FC_THROW(FC_ERR_ARG, "shape must have 1 to 3 entries");
+    const int nx = shape[len - 1];
+    const int ny = len >= 2 ? shape[len - 2] : 1;
+    const int nz = len == 3 ? shape[0] : 1;
+    const Geom g = make_geom(nx, ny, nz, nx, ny, nz, false);
+    const size_t b = plain_layout(g, false).total + 2 * sizeof(float) * (size_t)g.N();
+    mb = (long long)(b >> 20);
+  });
+  return (int)mb;
+}
+
+int fc_release_device(int devCUDA) {
+  clear_status();
+  return guarded([&] {
+    std::unique_ptr<DevCtx> c;
+    {
+      std::lock_guard<std::mutex> lk(g_ctx_mu);
+      auto it = g_ctx.find(devCUDA);
+      if (it == g_ctx.end()) return;
+      c = std::move(it->second);
+      g_ctx.erase(it);
+    }
+    std::lock_guard<std::mutex> lk(c->mu);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(devCUDA);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->ws);
+    cudaFree(c->d_img);
+    cudaFree(c->d_ker);
+    for (auto& kv : c->twiddles) cudaFree(kv.second);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    cudaSetDevice(prev);
+  });
+}
+
+size_t fc_conv3d_workspace_bytes(const int* imDim, const int* kernelDim, int flags) {
+  clear_status();
+  size_t r = 0;
+  guarded([&] {
+    int nx, ny, nz, kx = 0, ky = 0, kz = 0;
+    dims3(imDim, &nx, &ny, &nz);
+    const bool dense = flags & FC_FLAG_DENSE_KERNEL;
+    if (!dense) dims3(kernelDim, &kx, &ky, &kz);
+    const Geom g = make_geom(nx, ny, nz, kx, ky, kz, dense);
+    r = plain_layout(g, (flags & FC_FLAG_SHIFT_COMPAT) != 0).total;
+  });
+  return r;
+}
+
+int fc_conv3d_device(const float* d_image, float* d_out, const int* imDim, const float* d_kernel,
+                     const int* kernelDim, int flags, void* d_workspace, size_t workspace_bytes, void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_image || !d_out || !d_kernel) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    if (flags & (FC_FLAG_TC_FP16 | FC_FLAG_TC_BF16)) FC_THROW(FC_ERR_UNSUPPORTED, "tensor-core mode not built yet");
+    int nx, ny, nz, kx = 0, ky = 0, kz = 0;
+    dims3(imDim, &nx, &ny, &nz);
+    const bool dense = flags & FC_FLAG_DENSE_KERNEL;
+    if (!dense) dims3(kernelDim, &kx, &ky, &kz);
+    const Geom g = make_geom(nx, ny, nz, kx, ky, kz, dense);
+    const bool compat = (flags & FC_FLAG_SHIFT_COMPAT) && g.kbox;
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t wsb = workspace_bytes;
+    void* ws = resolve_ws(c, d_workspace, &wsb, plain_layout(g, compat).total);
+    enqueue_conv(c, g, d_image, d_out, d_kernel, compat, (char*)ws, wsb, (cudaStream_t)stream);
+  });
+}
+
+size_t fc_conv3d_adjoint_workspace_bytes(const int* imDim, const int* kernelDim, int flags) {
+  clear_status();
+  size_t r = 0;
+  guarded([&] {
+    int nx, ny, nz, kx = 0, ky = 0, kz = 0;
+    dims3(imDim, &nx, &ny, &nz);
+    const bool dense = flags & FC_FLAG_DENSE_KERNEL;
+    if (!dense) dims3(kernelDim, &kx, &ky, &kz);
+    r = adj_layout(make_geom(nx, ny, nz, kx, ky, kz, dense)).total;
+  });
+  return r;
+}
+
+int fc_conv3d_adjoint_device(const float* d_image, const float* d_kernel, const float* d_grad_out,
+                             float* d_grad_image, float* d_grad_kernel, const int* imDim, const int* kernelDim,
+                             int flags, void* d_workspace, size_t workspace_bytes, void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_grad_out) FC_THROW(FC_ERR_ARG, "NULL gradient");
+    if (d_grad_image && !d_kernel) FC_THROW(FC_ERR_ARG, "the image gradient needs the kernel");
+    if (d_grad_kernel && !d_image) FC_THROW(FC_ERR_ARG, "the kernel gradient needs the image");
+    if (flags & FC_FLAG_SHIFT_COMPAT)
+      FC_THROW(FC_ERR_UNSUPPORTED, "the adjoint is defined for the centred placement only");
+    int nx, ny, nz, kx = 0, ky = 0, kz = 0;
+    dims3(imDim, &nx, &ny, &nz);
+    const bool dense = flags & FC_FLAG_DENSE_KERNEL;
+    if (!dense) dims3(kernelDim, &kx, &ky, &kz);
+    const Geom g = make_geom(nx, ny, nz, kx, ky, kz, dense);
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t wsb = workspace_bytes;
+    void* ws = resolve_ws(c, d_workspace, &wsb, adj_layout(g).total);
+    if (!d_grad_image && !d_grad_kernel) return;
+    enqueue_adjoint(c, g, d_image, d_kernel, d_grad_out, d_grad_image, d_grad_kernel, (char*)ws, wsb,
+                    (cudaStream_t)stream);
+  });
+}
+
+size_t fc_fft3d_workspace_bytes(const int* imDim) {
+  clear_status();
+  size_t r = 0;
+  guarded([&] {
+    int nx, ny, nz;
+    dims3(imDim, &nx, &ny, &nz);
+    r = fft_ws_bytes(make_geom(nx, ny, nz, 0, 0, 0, true));
+  });
+  return r;
+}
+
+int fc_rfft3d_device(const float* d_in, float* d_spec, const int* imDim, void* d_workspace, size_t workspace_bytes,
+                     void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_in || !d_spec) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    int nx, ny, nz;
+    dims3(imDim, &nx, &ny, &nz);
+    const Geom g = make_geom(nx, ny, nz, 0, 0, 0, true);
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t wsb = workspace_bytes;
+    void* ws = resolve_ws(c, d_workspace, &wsb, fft_ws_bytes(g));
+    enqueue_rfft3d(c, g, d_in, d_spec, (char*)ws, wsb, (cudaStream_t)stream);
+  });
+}
+
+int fc_irfft3d_device(const float* d_spec, float* d_out, const int* imDim, void* d_workspace, size_t workspace_bytes,
+                      void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_spec || !d_out) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    int nx, ny, nz;
+    dims3(imDim, &nx, &ny, &nz);
+    const Geom g = make_geom(nx, ny, nz, 0, 0, 0, true);
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t wsb = workspace_bytes;
+    void* ws = resolve_ws(c, d_workspace, &wsb, fft_ws_bytes(g));
+    enqueue_irfft3d(c, g, d_spec, d_out, (char*)ws, wsb, (cudaStream_t)stream);
+  });
+}
+
+int fc_pad_shift_kernel_device(const float* d_kernel, const int* kernelDim, const int* imDim, int flags,
+                               float* d_out, void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_kernel || !d_out) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    int nx, ny, nz, kx, ky, kz;
+    dims3(imDim, &nx, &ny, &nz);
+    dims3(kernelDim, &kx, &ky, &kz);
+    const Geom g = make_geom(nx, ny, nz, kx, ky, kz, false);
+    cudaStream_t st = (cudaStream_t)stream;
+    cuda_check(cudaMemsetAsync(d_out, 0, sizeof(float) * (size_t)g.N(), st), "cudaMemsetAsync");
+    FC_PASS("pad_shift", 8.0 * kx * ky * kz, st,
+            launch_pad_shift(d_kernel, kx, ky, kz, nx, ny, nz, (flags & FC_FLAG_SHIFT_COMPAT) != 0, d_out, st));
+  });
+}
+
+size_t fc_conv3d_batched_workspace_bytes(int n_views, const int* dims, int flags) {
+  clear_status();
+  size_t r = 0;
+  guarded([&] {
+    if (n_views < 1 || !dims) FC_THROW(FC_ERR_ARG, "no views");
+    for (int v = 0; v < n_views; ++v) {
+      const int* d = dims + 6 * v;
+      const Geom g = make_geom(d[0], d[1], d[2], d[3], d[4], d[5], false);
+      r += plain_layout(g, (flags & FC_FLAG_SHIFT_COMPAT) != 0).total;
+    }
+  });
+  return r;
+}
+
+int fc_conv3d_batched_device(int n_views, const float* const* d_images, float* const* d_outs,
+                             const float* const* d_kernels, const int* dims, int flags, void* d_workspace,
+                             size_t workspace_bytes, void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (n_views < 1 || !d_images || !d_outs || !d_kernels || !dims) FC_THROW(FC_ERR_ARG, "NULL argument");
+    const bool compat = (flags & FC_FLAG_SHIFT_COMPAT) != 0;
+    std::vector<Geom> gs;
+    size_t need = 0;
+    for (int v = 0; v < n_views; ++v) {
+      const int* d = dims + 6 * v;
+      gs.push_back(make_geom(d[0], d[1], d[2], d[3], d[4], d[5], false));
+      need += plain_layout(gs.back(), compat).total;
+    }
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t wsb = workspace_bytes;
+    char* ws = (char*)resolve_ws(c, d_workspace, &wsb, need);
+    size_t off = 0;
+    for (int v = 0; v < n_views; ++v) {
+      const size_t b = plain_layout(gs[v], compat).total;
+      enqueue_conv(c, gs[v], d_images[v], d_outs[v], d_kernels[v], compat, ws + off, b, (cudaStream_t)stream);
+      off += b;
+    }
+  });
+}
+
+void fc_profile_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_on = on != 0;
+}
+
+int fc_profile_read(char* names, int name_stride, float* ms, double* bytes, int max) {
+  std::vector<ProfRec> recs;
+  {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    recs.swap(g_prof);
+  }
+  int n = 0;
+  for (auto& r : recs) {
+    cudaEventSynchronize(r.b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, r.a, r.b);
+    if (n < max) {
+      if (names && name_stride > 0) {
+        std::strncpy(names + (size_t)n * name_stride, r.name.c_str(), name_stride - 1);
+        names[(size_t)n * name_stride + name_stride - 1] = 0;
+      }
+      if (ms) ms[n] = t;
+      if (bytes) bytes[n] = r.bytes;
+      ++n;
+    }
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// Internal declarations shared by the host orchestration (fc_host.cpp) and
+// the kernel launchers (fc_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include "fc_axis.h"
+
+namespace fc {
+
+// Geometry of one circular convolution: image nx*ny*nz (x fastest), kernel
+// source either a kx*ky*kz box of taps placed by the centred circular shift
+// (kmode_box) or an image-sized dense real array (already shifted).
+struct Geom {
+  int nx, ny, nz;
+  int kx, ky, kz;      // box dims (box mode); nx,ny,nz in dense mode
+  int nxh;             // nx/2 + 1 complex values per spectrum row
+  long long pitch;     // complex values between spectrum rows (>= nxh)
+  bool kbox;           // true: box of taps, false: dense N-float kernel
+  int kplanes;         // z-planes of the kernel spectrum actually computed (kz or nz)
+  int krows;           // rows per kernel plane carried by the x pass (ky or ny)
+  long long N() const { return (long long)nx * ny * nz; }
+};
+
+struct Tiles {
+  int x_pairs_log2;   // row pairs per CTA in the x passes
+  int y_cols_log2;    // columns per tile in the y passes
+  int z_cols_log2;    // columns per tile in the fused z pass
+  int threads;        // threads per CTA
+};
+
+// Workspace layout (byte offsets from the workspace base, 256-aligned)
+struct Layout {
+  size_t off_S, off_KX, off_KXY, off_dense, off_aux, total;
+};
+
+// Launch helpers (fc_kernels.cu).  All enqueue on `st`; none synchronise.
+// Each returns cudaGetLastError() of its launch(es).
+cudaError_t launch_x_r2c_dense(const float* in, long long in_pitch, float2* out, long long out_pitch, long long nrows,
+                               const FcAxis& ax, const Tiles& t, cudaStream_t st);
+cudaError_t launch_x_r2c_box(const float* taps, int kx, int hx, float2* out, long long out_pitch, long long nrows,
+                             const FcAxis& ax, const Tiles& t, cudaStream_t st);
+cudaError_t launch_x_c2r(const float2* in, long long in_pitch, float* out, long long out_pitch, long long nrows,
+                         const FcAxis& ax, const Tiles& t, cudaStream_t st);
+// Column FFT over axis `ax`: element (plane, j, c) at base + plane*ps + j*es + c,
+// c in [0, ncols).  In place when src == dst.
+cudaError_t launch_cols(const float2* src, float2* dst, long long ps, long long es, int ncols, int nplanes,
+                        bool inverse, const FcAxis& ax, int cols_log2, int threads, cudaStream_t st);
+// Kernel y pass: source rows are the compact x-spectrum rows iy in [0,krows) of
+// each plane, y maps to iy = (y + hy) mod ny (rows outside are zero).
+cudaError_t launch_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
+                           int nplanes, const FcAxis& ax, int cols_log2, int threads, cudaStream_t st);
+// Fused z pass: z-forward of the image column and the kernel column, the
+// reference's modulate-and-normalise (kernel * image * scale), z-inverse.
+// conj_kernel: multiply by conj(kernel spectrum) (adjoint / correlation).
+cudaError_t launch_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+                         float scale, bool conj_kernel, const FcAxis& az, int cols_log2, int threads,
+                         cudaStream_t st);
+// Kernel-gradient z pass: z-forward of image spectrum X and gradient spectrum G
+// columns, conj(X) * G * scale, z-inverse, and keep only the kz planes of the
+// kernel support: out plane p <- z = (p - hz) mod nz.
+cudaError_t launch_zcorr_crop(const float2* X, const float2* G, float2* out, long long pitch, int ny, int ncols,
+                              int kz, int hz, float scale, const FcAxis& az, int cols_log2, int threads,
+                              cudaStream_t st);
+// Scatter of the kernel taps into a dense zeroed N-float buffer (x fastest).
+//   compat = false : centred circular shift
+//   compat = true  : the reference's fftShiftKernel arithmetic as called from
+//                    its in-place entry point
+cudaError_t launch_pad_shift(const float* taps, int kx, int ky, int kz, int nx, int ny, int nz, bool compat,
+                             float* out, cudaStream_t st);
+// Crop/gather for the kernel gradient: out[iz][iy][ix] = vol[(iz-hz)%nz][(iy-hy)%ny][(ix-hx)%nx]
+// from a real volume whose rows have `pitch` floats and whose planes are
+// given by a compact array of kz planes (plane p holds z = (p - hz) mod nz).
+cudaError_t launch_crop_kernel(const float* vol, long long row_pitch, int ny_rows, int nx, int kx, int ky, int kz,
+                               float* out, cudaStream_t st);
+
+// reference thread-count helper (src/convolution3Dfft.cu:26-38) restated for
+// the compat scatter's grid truncation
+int ref_closest_multiplier(int a_number, int multiplier);
+
+}  // namespace fc
