@@ -193,7 +193,7 @@ def fft_conv_fp64(image: np.ndarray, padded_kernel: np.ndarray) -> np.ndarray:
     """Circular convolution in double precision: irfftn(rfftn(im) * rfftn(k))."""
     a = np.fft.rfftn(np.asarray(image, np.float64))
     b = np.fft.rfftn(np.asarray(padded_kernel, np.float64))
-    return np.fft.irfftn(a * b, s=image.shape)
+    return np.fft.irfftn(a * b, s=image.shape, axes=(0, 1, 2))
 
 
 def conv_fp64(image: np.ndarray, kernel: np.ndarray, placement: str = "centered") -> np.ndarray:
@@ -233,7 +233,8 @@ def reference_path_fp32(image: np.ndarray, kernel: np.ndarray, placement: str = 
     kspec = np.ascontiguousarray(kspec, np.complex64)
     nthreads = os.cpu_count() if workers in (-1, None) else workers
     modulate_and_normalize(spec, kspec, np.float32(1.0) / np.float32(im.size), threads=nthreads)
-    return np.asarray(sfft.irfftn(spec, s=im.shape, workers=workers), np.float32)
+    # norm='forward' leaves the inverse unscaled, as cuFFT's C2R is (the 1/N is in the multiply)
+    return np.asarray(sfft.irfftn(spec, s=im.shape, workers=workers, norm="forward"), np.float32)
 
 
 # ------------------------------------------------------------------ padding utilities
@@ -380,58 +381,3 @@ def kat_cases(include_large: bool = True) -> List[dict]:
                           expected=stack.copy(), reference_expected=2 * stack, metric="l2norm", threshold=thr,
                           cite="tests/test_gpu_numerical_stability.cpp:222-382"))
     return cases
-
-
-# ------------------------------------------------------------------ synthetic microscope volumes
-def spot_volume(shape_zyx: Sequence[int], n_spots: int, seed: int, background: float = 100.0,
-                sigma: float = 2.0, amp: Tuple[float, float] = (200.0, 2000.0), poisson: bool = True) -> np.ndarray:
-    """Background + Gaussian spots (uniform centres, uniform amplitudes), then
-    Poisson noise; generated in float64 from numpy's PCG64 and cast to float32."""
-    rng = np.random.Generator(np.random.PCG64(seed))
-    nz, ny, nx = shape_zyx
-    vol = np.full((nz, ny, nx), background, np.float64)
-    cz = rng.uniform(0, nz, n_spots)
-    cy = rng.uniform(0, ny, n_spots)
-    cx = rng.uniform(0, nx, n_spots)
-    a = rng.uniform(amp[0], amp[1], n_spots)
-    r = int(np.ceil(4 * sigma))
-    off = np.arange(-r, r + 1)
-    for z0, y0, x0, aa in zip(cz, cy, cx, a):
-        iz = (np.floor(z0).astype(int) + off) % nz
-        iy = (np.floor(y0).astype(int) + off) % ny
-        ix = (np.floor(x0).astype(int) + off) % nx
-        gz = np.exp(-0.5 * ((np.floor(z0) + off - z0) / sigma) ** 2)
-        gy = np.exp(-0.5 * ((np.floor(y0) + off - y0) / sigma) ** 2)
-        gx = np.exp(-0.5 * ((np.floor(x0) + off - x0) / sigma) ** 2)
-        vol[np.ix_(iz, iy, ix)] += aa * gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
-    if poisson:
-        vol = rng.poisson(vol).astype(np.float64)
-    return vol.astype(np.float32)
-
-
-def gaussian_psf(shape_zyx: Sequence[int], sigma_zyx: Sequence[float], rotation: Optional[np.ndarray] = None,
-                 mix: Optional[Iterable[Tuple[float, Sequence[float]]]] = None) -> np.ndarray:
-    """Anisotropic Gaussian PSF (optionally rotated, or a weighted mixture of
-    Gaussians), normalised to sum 1, float32."""
-    kz, ky, kx = shape_zyx
-    z, y, x = np.meshgrid(np.arange(kz) - kz // 2, np.arange(ky) - ky // 2, np.arange(kx) - kx // 2, indexing="ij")
-    pts = np.stack([z, y, x], -1).astype(np.float64)
-    if rotation is not None:
-        pts = pts @ rotation.T
-    comps = list(mix) if mix is not None else [(1.0, sigma_zyx)]
-    g = np.zeros((kz, ky, kx))
-    for w, s in comps:
-        s = np.asarray(s, np.float64)
-        g += w * np.exp(-0.5 * np.sum((pts / s) ** 2, -1))
-    g /= g.sum()
-    return g.astype(np.float32)
-
-
-def euler_zyz(a: float, b: float, c: float) -> np.ndarray:
-    def rz(t):
-        return np.array([[1, 0, 0], [0, np.cos(t), -np.sin(t)], [0, np.sin(t), np.cos(t)]])  # about z in (z,y,x)
-
-    def ry(t):
-        return np.array([[np.cos(t), 0, np.sin(t)], [0, 1, 0], [-np.sin(t), 0, np.cos(t)]])
-
-    return rz(a) @ ry(b) @ rz(c)

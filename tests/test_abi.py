@@ -1,0 +1,130 @@
+"""The C ABI library without a GPU: it loads, exports exactly what
+include/convolution3Dfft.h declares, and its host-only logic (radix plans,
+scratch estimates, argument validation) behaves.  No compute call is made."""
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "convolution3Dfft.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = "\n".join(ln for ln in text.splitlines() if not ln.lstrip().startswith("#"))
+    names = re.findall(r"FUNCTION_PREFIX\s+[\w\s\*]+?\b(\w+)\s*\(", text)
+    return sorted(set(names))
+
+
+REFERENCE_EXPORTS = [  # reference src/convolution3Dfft.h:29-84
+    "convolution3DfftCUDA_test", "convolution3DfftCUDA", "convolution3DfftCUDAInPlace",
+    "selectDeviceWithHighestComputeCapability", "getCUDAcomputeCapabilityMinorVersion",
+    "getCUDAcomputeCapabilityMajorVersion", "getNumDevicesCUDA", "getNameDeviceCUDA", "getMemDeviceCUDA",
+    "cuda_version", "gpu_mem_needed_mb",
+]
+
+
+def test_header_declares_reference_exports():
+    decl = declared_functions()
+    for name in REFERENCE_EXPORTS:
+        assert name in decl, name
+
+
+def test_library_exports_every_declared_symbol(fclib):
+    import fourierconvolutioncudalib_gb300 as fc
+
+    path = fc.library_path()
+    out = subprocess.run(["nm", "-D", "--defined-only", str(path)], capture_output=True, text=True, check=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    decl = set(declared_functions())
+    assert decl <= exported, decl - exported
+    # nothing else leaks out of the library (hidden visibility)
+    assert exported <= decl, exported - decl
+    for name in decl:
+        assert hasattr(fclib, name)
+
+
+def test_library_named_for_jna(fclib):
+    import fourierconvolutioncudalib_gb300 as fc
+
+    assert fc.library_path().name == "libFourierConvolutionCUDALib.so"
+
+
+def test_plan_radices(fclib):
+    import fourierconvolutioncudalib_gb300 as fc
+
+    assert fc.plan_radices(512) == [8, 8, 8]
+    assert fc.plan_radices(128) == [16, 8]
+    assert fc.plan_radices(256) == [16, 16]
+    assert fc.plan_radices(384) == [16, 8, 3]
+    assert fc.plan_radices(448) == [8, 8, 7]
+    assert fc.plan_radices(96) == [8, 4, 3]
+    assert fc.plan_radices(352) == [8, 4, 11]
+    assert fc.plan_radices(218) == [2, 109]
+    assert fc.plan_radices(13 * 17) == [13, 17]
+    assert fc.plan_radices(1) == [1]
+    for n in (2, 3, 60, 343, 1000, 1024, 4096, 158, 148, 168, 4093):
+        r = fc.plan_radices(n)
+        assert int(np.prod(r)) == n
+
+
+def test_gpu_mem_needed_is_host_only(fclib):
+    import fourierconvolutioncudalib_gb300 as fc
+
+    mb = fc.gpu_mem_needed_mb([128, 512, 512])
+    # spectrum + kernel spectrum (same size here) + image + kernel: ~ 4 x 140 MB
+    assert 400 < mb < 700
+    assert fc.gpu_mem_needed_mb([64]) >= 0
+    assert fc.lib().gpu_mem_needed_mb(fc._iarr([0, 4, 4]), 3) == -1
+    assert fc.lib().fc_last_status() == fc.FC_ERR_ARG
+
+
+def test_workspace_bytes_monotone(fclib):
+    import fourierconvolutioncudalib_gb300 as fc
+
+    L = fc.lib()
+    a = L.fc_conv3d_workspace_bytes(fc._iarr([512, 512, 128]), fc._iarr([31, 31, 63]), 0)
+    b = L.fc_conv3d_workspace_bytes(fc._iarr([512, 512, 128]), fc._iarr([63, 63, 127]), 0)
+    c = L.fc_conv3d_workspace_bytes(fc._iarr([512, 512, 128]), fc._iarr([31, 31, 63]), fc.FC_FLAG_SHIFT_COMPAT)
+    assert 0 < a < b <= c
+    assert L.fc_conv3d_workspace_bytes(fc._iarr([512, 512, 128]), fc._iarr([513, 1, 1]), 0) == 0
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+
+
+def test_argument_validation_without_gpu(fclib):
+    """Invalid calls fail with a status before any device work, and never exit."""
+    import fourierconvolutioncudalib_gb300 as fc
+
+    L = fc.lib()
+    im = np.ones((4, 4, 4), np.float32)
+    k = np.ones((3, 3, 3), np.float32)
+    FP = ctypes.POINTER(ctypes.c_float)
+    L.convolution3DfftCUDAInPlace(None, fc._iarr([4, 4, 4]), k.ctypes.data_as(FP), fc._iarr([3, 3, 3]), 0)
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    L.convolution3DfftCUDAInPlace(im.ctypes.data_as(FP), fc._iarr([4, 0, 4]), k.ctypes.data_as(FP),
+                                  fc._iarr([3, 3, 3]), 0)
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    L.convolution3DfftCUDAInPlace(im.ctypes.data_as(FP), fc._iarr([4, 4, 4]), k.ctypes.data_as(FP),
+                                  fc._iarr([5, 3, 3]), 0)
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    assert np.all(im == 1)
+    assert not L.convolution3DfftCUDA(im.ctypes.data_as(FP), None, k.ctypes.data_as(FP), fc._iarr([3, 3, 3]), 0)
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    assert L.fc_conv3d_device(None, None, fc._iarr([4, 4, 4]), None, fc._iarr([3, 3, 3]), 0, None, 0, None) == \
+        fc.FC_ERR_ARG
+    msg = L.fc_last_error().decode()
+    assert "NULL" in msg
+    with pytest.raises(fc.FcError):
+        fc.convolution3DfftCUDAInPlace(im, (4, 4, 4), np.ones((3, 3), np.float32), (3, 3, 1), 0)
+
+
+def test_version_and_cuda_version(fclib):
+    import fourierconvolutioncudalib_gb300 as fc
+
+    assert b"sm_103a" in fc.lib().fc_version()
+    assert fc.cuda_version() >= 13000
