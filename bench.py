@@ -1,0 +1,427 @@
+#!/usr/bin/env python
+"""Benchmark of the 3D FFT convolution on GB300.
+
+Workload (default): the plain forward convolution at microscope size -- a
+512x512x128 (x,y,z) float32 stack (background 100 + 2000 Gaussian spots,
+Poisson noise, seed 2) with a 31x31x63 anisotropic Gaussian PSF.  One step is
+one full convolution (kernel spectrum + image transforms + product + inverse)
+of that volume.  Inputs are seeded synthetic data of the configuration's
+shapes and value distribution.
+
+Line fields (one JSON line from rank 0):
+  value     Gvoxel/s with inputs resident in HBM (fc_conv3d_device), per-step
+            CUDA events on the launch stream, L2 flushed before every step
+            (256 MiB write, outside the step events), mean over K steps, max
+            over ranks; whole-job aggregate over N replicas.
+  e2e       the same metric through convolution3DfftCUDAInPlace with host
+            buffers (pinned), H2D + compute + D2H inside the timed call.
+  roofline  the dominant pass, algorithmic bytes / its mean event duration,
+            against the measured HBM copy bandwidth.
+  cpu_baseline  the reference algorithm on the host cores (oracle port).
+  ref_cufft the reference's device sequence (cuFFT R2C x2, modulate, C2R)
+            on the same GPU, for comparison.
+`--impl reference` times the reference algorithm on the host instead (the
+oracle's float32 port; the reference library itself needs cuFFT on a GPU and
+its sources are not on the GPU host).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CONFIGS = {
+    "c2a": dict(workload="plain_conv_512x512x128_psf31x31x63", fn="c2", kw=dict(nonpow2=False)),
+    "c2b": dict(workload="plain_conv_384x448x96_psf31x31x63", fn="c2", kw=dict(nonpow2=True)),
+    "c1": dict(workload="plain_conv_64x64x64_psf7x7x7", fn="c1", kw={}),
+    "c5": dict(workload="plain_conv_1024x1024x256_psf63x63x63", fn="c5", kw={}),
+}
+METRIC = "Gvoxel/s per 3D FFT conv (plain/batched/adjoint/TC) vs plain & ref cuFFT, rel-L2<=1e-5"
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append((time.perf_counter(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.t:
+            self.t.join(timeout=5)
+
+    def summary(self, t0: float, t1: float):
+        inside = [r for t, r in self.rows if t0 <= t <= t1] or [r for _, r in self.rows]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in inside if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in inside if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in inside for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(inside)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if os.environ.get("FC_BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return world, rank, local
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def make_data(cfg):
+    from fourierconvolutioncudalib_gb300 import workloads as W
+
+    return getattr(W, cfg["fn"])(**cfg["kw"])
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args, cfg, world, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+
+    d = make_data(cfg)
+    im, k = d["image"], d["kernel"]
+    cores = os.cpu_count() or 1
+    budget_s = float(os.environ.get("FC_BENCH_REF_BUDGET_S", "120"))
+    t = time.perf_counter()
+    orc.reference_path_fp32(im, k, "centered", workers=cores)
+    first = time.perf_counter() - t
+    warm = min(args.warmup, max(0, int(10 / max(first, 1e-3))))
+    for _ in range(warm):
+        orc.reference_path_fp32(im, k, "centered", workers=cores)
+    steps = max(1, min(args.steps, int(budget_s / max(first, 1e-3))))
+    times = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        orc.reference_path_fp32(im, k, "centered", workers=cores)
+        times.append(time.perf_counter() - t)
+    ms = 1e3 * statistics.mean(times)
+    val = im.size / (ms / 1e3) / 1e9
+    sample = f"{steps} full-volume steps of {args.steps} requested (budget {budget_s:.0f} s), {warm} warm-up"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "Gvoxel/s", "n_gpus": world, "steps": steps,
+        "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded, configuration shapes)",
+        "config": {"workload": cfg["workload"], "image_xyz": list(im.shape[::-1]), "kernel_xyz": list(k.shape[::-1]),
+                   "impl_detail": "reference algorithm on host cores: pad+shift, R2C x2, modulate 1/N, C2R "
+                                  "(float32, scipy.fft transforms standing in for cuFFT)"},
+        "cpu_baseline": {"value": val, "unit": "Gvoxel/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "Gvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, cfg, world, rank, local):
+    import torch
+
+    import fourierconvolutioncudalib_gb300 as fc
+    from fourierconvolutioncudalib_gb300 import build as fcbuild
+    from fourierconvolutioncudalib_gb300 import device as fcd
+
+    fcbuild.build()
+    fc.load_library()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    d = make_data(cfg)
+    im_np, k_np = d["image"], d["kernel"]
+    nz, ny, nx = im_np.shape
+    kz, ky, kx = k_np.shape
+    N = im_np.size
+    img = torch.from_numpy(im_np).to(dev)
+    ker = torch.from_numpy(k_np).to(dev)
+    out = torch.empty_like(img)
+    ws = torch.empty(fcd.workspace_bytes(im_np.shape, k_np.shape), dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        fcd.conv3d(img, ker, out=out, workspace=ws)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, per-step events, per-pass events (library profiling)
+    K = args.steps
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    fcd.profile(True)
+    launches = 0
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(K):
+        flush.zero_()
+        evs[i][0].record(stream)
+        step()
+        evs[i][1].record(stream)
+        launches += fcd.launch_count()
+    torch.cuda.synchronize()
+    barrier(world)
+    t1 = time.perf_counter()
+    fcd.profile(False)
+    time.sleep(0.2)
+    clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    passes = fcd.profile()
+    ms_local = statistics.mean(step_ms)
+    ms = reduce_max(ms_local, world)
+    value = world * N / (ms / 1e3) / 1e9
+
+    # per-pass means -> dominant kernel roofline
+    peak, peak_kind = load_peaks()
+    agg = {}
+    for name, pms, by in passes:
+        a = agg.setdefault(name, [0.0, 0.0, 0])
+        a[0] += pms
+        a[1] += by
+        a[2] += 1
+    table = []
+    for name, (tms, tby, cnt) in agg.items():
+        mean_ms = tms / cnt
+        gbs = (tby / cnt) / (mean_ms / 1e3) / 1e9 if mean_ms > 0 else 0.0
+        table.append({"pass": name, "launches": cnt, "mean_us": 1e3 * mean_ms, "alg_bytes": tby / cnt, "GB/s": gbs,
+                      "frac": gbs / peak})
+    table.sort(key=lambda r: -r["mean_us"] * r["launches"])
+    dom = table[0] if table else None
+    traffic = None
+    tf = ROOT / "profiles" / "ncu_traffic.json"
+    if dom and tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(cfg["workload"], {}).get(dom["pass"])
+        except Exception:
+            traffic = None
+    Mc = (nx // 2 + 1) * ny * nz
+    model_bytes = 8 * N + 4 * k_np.size + 80 * Mc
+    roofline = {"bound": "hbm", "kernel": dom["pass"] if dom else None, "achieved": dom["GB/s"] if dom else None,
+                "peak": peak, "unit": "GB/s", "frac": dom["frac"] if dom else None, "traffic": traffic,
+                "peak_source": peak_kind,
+                "step_model_bytes": model_bytes, "step_model_frac": model_bytes / (ms / 1e3) / 1e9 / peak}
+
+    # ---- end to end through the reference-facing C ABI, host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = torch.empty(N, dtype=torch.float32, pin_memory=True).numpy().reshape(im_np.shape)
+        kpin = torch.empty(k_np.size, dtype=torch.float32, pin_memory=True).numpy().reshape(k_np.shape)
+        kpin[...] = k_np
+        e2e_t = []
+        page = im_np.copy()
+        page_t = []
+        reps = max(3, min(args.steps, 20))
+        for i in range(reps + 2):
+            np.copyto(pin, im_np)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fc.convolution3DfftCUDAInPlace(pin, (nx, ny, nz), kpin, (kx, ky, kz), local)
+            dt = time.perf_counter() - t
+            if i >= 2:
+                e2e_t.append(dt)
+        for i in range(min(reps, 5) + 1):
+            np.copyto(page, im_np)
+            t = time.perf_counter()
+            fc.convolution3DfftCUDAInPlace(page, (nx, ny, nz), k_np, (kx, ky, kz), local)
+            dt = time.perf_counter() - t
+            if i >= 1:
+                page_t.append(dt)
+        ok_err = float(np.max(np.abs(pin - out.cpu().numpy())) / max(1e-30, float(np.max(np.abs(pin)))))
+        e2e_s = reduce_max(statistics.median(e2e_t), world)
+        e2e = {"value": world * N / e2e_s / 1e9, "unit": "Gvoxel/s", "h2d_bytes_per_step": 4 * (N + k_np.size),
+               "d2h_bytes_per_step": 4 * N, "host_buffer": "pinned", "ms_per_call": 1e3 * e2e_s,
+               "pageable_ms_per_call": 1e3 * statistics.median(page_t), "api": "convolution3DfftCUDAInPlace",
+               "max_rel_diff_vs_device_path": ok_err}
+
+    # ---- reference device sequence on cuFFT, same GPU
+    ref_cufft = None
+    if not args.no_ref_cufft:
+        try:
+            ref_cufft = time_ref_cufft(im_np, k_np, dev, args, value)
+        except Exception as e:  # the cuFFT harness is optional for the line
+            ref_cufft = {"error": str(e)[:200]}
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = time_cpu_baseline(im_np, k_np)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gvoxel/s", "n_gpus": world, "steps": K,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, configuration shapes and distribution)",
+            "config": {"workload": cfg["workload"], "image_xyz": [nx, ny, nz], "kernel_xyz": [kx, ky, kz],
+                       "api": "fc_conv3d_device", "l2": "flushed before every step (256 MiB write outside the "
+                                                         "step events)", "parallelism": f"replicas x{world}"},
+            "wall_s_timed_region": t1 - t0,
+            "e2e": e2e, "roofline": roofline, "passes": table, "cpu_baseline": cpu, "ref_cufft": ref_cufft,
+            "gpu_launches": launches, "clocks": clocks.summary(t0, t1),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def time_ref_cufft(im_np, k_np, dev, args, our_value):
+    """The reference's device sequence (R2C image, R2C kernel, modulate, C2R) on
+    cuFFT with plans built beforehand, CUDA events around each sequence."""
+    import torch
+    from baseline import refseq
+
+    L = refseq.lib()
+    nz, ny, nx = im_np.shape
+    nxh = nx // 2 + 1
+    base_img = torch.zeros((nz, ny, 2 * nxh), dtype=torch.float32, device=dev)
+    base_img[..., :nx] = torch.from_numpy(im_np).to(dev)
+    kz, ky, kx = k_np.shape
+    pk = np.zeros(im_np.shape, np.float32)  # centred placement, same as the library's default
+    iz = (np.arange(kz) - kz // 2) % nz
+    iy = (np.arange(ky) - ky // 2) % ny
+    ix = (np.arange(kx) - kx // 2) % nx
+    pk[np.ix_(iz, iy, ix)] = k_np
+    base_ker = torch.zeros_like(base_img)
+    base_ker[..., :nx] = torch.from_numpy(pk).to(dev)
+    wi = torch.empty_like(base_img)
+    wk = torch.empty_like(base_img)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    st = torch.cuda.current_stream()
+    reps = max(3, min(args.steps, 50))
+    times = []
+    for i in range(reps + 3):
+        wi.copy_(base_img)
+        wk.copy_(base_ker)
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        rc = L.refseq_device_only(wi.data_ptr(), wk.data_ptr(), nx, ny, nz, st.cuda_stream)
+        b.record(st)
+        if rc != 0:
+            raise RuntimeError(L.refseq_last_error().decode())
+        torch.cuda.synchronize()
+        if i >= 3:
+            times.append(a.elapsed_time(b))
+    L.refseq_release()
+    ms = statistics.mean(times)
+    v = im_np.size / (ms / 1e3) / 1e9
+    return {"value": v, "unit": "Gvoxel/s", "ms_per_step": ms, "speedup_of_ours": our_value / v,
+            "what": "cuFFT 3D R2C(image), R2C(padded kernel), modulate x 1/N, C2R; plans pre-built"}
+
+
+def time_cpu_baseline(im_np, k_np):
+    from oracle import oracle as orc
+
+    cores = os.cpu_count() or 1
+    t = time.perf_counter()
+    orc.reference_path_fp32(im_np, k_np, "centered", workers=cores)
+    first = time.perf_counter() - t
+    n = max(1, min(5, int(15.0 / max(first, 1e-3))))
+    ts = []
+    for _ in range(n):
+        t = time.perf_counter()
+        orc.reference_path_fp32(im_np, k_np, "centered", workers=cores)
+        ts.append(time.perf_counter() - t)
+    s = statistics.mean(ts)
+    return {"value": im_np.size / s / 1e9, "unit": "Gvoxel/s", "cores": cores, "kind": "port",
+            "sample": f"{n} full-volume convolutions (after 1 warm-up): the reference algorithm in float32 on the "
+                      f"host, scipy.fft transforms on {cores} threads"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="c2a")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ref-cufft", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    cfg = CONFIGS[args.config]
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, cfg, world, rank)
+    else:
+        run_ours(args, cfg, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -314,6 +314,55 @@ struct PassScope {
     ++t_launches;                                     \
   } while (0)
 
+// ------------------------------------------------------------------ fast / generic dispatch
+// The register-resident kernels cover power-of-two lengths; every other
+// length runs on the generic shared-memory kernels.  FC_GENERIC=1 forces the
+// generic kernels everywhere (used by the tests to cover both).
+static int g_generic_only = -1;
+static bool use_fast() {
+  if (g_generic_only < 0) {
+    const char* e = std::getenv("FC_GENERIC");
+    g_generic_only = (e && std::atoi(e) != 0) ? 1 : 0;
+  }
+  return g_generic_only == 0;
+}
+
+static cudaError_t d_x_r2c_dense(const float* in, long long ip, float2* out, long long op, long long rows,
+                                 const FcAxis& ax, const Tiles& t, cudaStream_t st) {
+  if (use_fast() && fast_rows_supported(ax.n)) return fast_x_r2c_dense(in, ip, out, op, rows, ax, st);
+  return launch_x_r2c_dense(in, ip, out, op, rows, ax, t, st);
+}
+static cudaError_t d_x_r2c_box(const float* taps, int kx, int hx, float2* out, long long op, long long rows,
+                               const FcAxis& ax, const Tiles& t, cudaStream_t st) {
+  if (use_fast() && fast_rows_supported(ax.n)) return fast_x_r2c_box(taps, kx, hx, out, op, rows, ax, st);
+  return launch_x_r2c_box(taps, kx, hx, out, op, rows, ax, t, st);
+}
+static cudaError_t d_x_c2r(const float2* in, long long ip, float* out, long long op, long long rows, const FcAxis& ax,
+                           const Tiles& t, cudaStream_t st) {
+  if (use_fast() && fast_rows_supported(ax.n)) return fast_x_c2r(in, ip, out, op, rows, ax, st);
+  return launch_x_c2r(in, ip, out, op, rows, ax, t, st);
+}
+static cudaError_t d_cols(const float2* src, float2* dst, long long ps, long long es, int ncols, int nplanes, bool inv,
+                          const FcAxis& ax, int cols_log2, int threads, cudaStream_t st) {
+  if (use_fast() && fast_cols_supported(ax.n)) return fast_cols(src, dst, ps, es, ncols, nplanes, inv, ax, st);
+  return launch_cols(src, dst, ps, es, ncols, nplanes, inv, ax, cols_log2, threads, st);
+}
+static cudaError_t d_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
+                             int nplanes, const FcAxis& ax, int cols_log2, int threads, cudaStream_t st) {
+  if (use_fast() && fast_cols_supported(ax.n)) return fast_cols_kx(kx_spec, pitch, krows, hy, dst, ncols, nplanes, ax, st);
+  return launch_cols_kx(kx_spec, pitch, krows, hy, dst, ncols, nplanes, ax, cols_log2, threads, st);
+}
+static cudaError_t d_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+                           float scale, bool conj, const FcAxis& az, int cols_log2, int threads, cudaStream_t st) {
+  if (use_fast() && fast_cols_supported(az.n)) return fast_zconv(S, KXY, pitch, ny, ncols, kplanes, hz, scale, conj, az, st);
+  return launch_zconv(S, KXY, pitch, ny, ncols, kplanes, hz, scale, conj, az, cols_log2, threads, st);
+}
+static cudaError_t d_zcorr(const float2* X, const float2* G, float2* out, long long pitch, int ny, int ncols, int kz,
+                           int hz, float scale, const FcAxis& az, int cols_log2, int threads, cudaStream_t st) {
+  if (use_fast() && fast_cols_supported(az.n)) return fast_zcorr(X, G, out, pitch, ny, ncols, kz, hz, scale, az, st);
+  return launch_zcorr_crop(X, G, out, pitch, ny, ncols, kz, hz, scale, az, cols_log2, threads, st);
+}
+
 // ------------------------------------------------------------------ pass chains
 struct Axes {
   FcAxis x, y, z;
@@ -336,15 +385,15 @@ static void enqueue_kernel_spectrum(const Geom& g, const Axes& a, const Tiles& t
   if (g.kbox) {
     const long long rows = (long long)g.kplanes * g.krows;
     FC_PASS("kernel_x_r2c", 4.0 * g.kx * rows + 8.0 * g.nxh * rows, st,
-            launch_x_r2c_box(d_kernel, g.kx, g.kx / 2, KX, g.pitch, rows, a.x, t, st));
+            d_x_r2c_box(d_kernel, g.kx, g.kx / 2, KX, g.pitch, rows, a.x, t, st));
     FC_PASS("kernel_y_fwd", 8.0 * g.nxh * (rows + (double)g.ny * g.kplanes), st,
-            launch_cols_kx(KX, g.pitch, g.krows, g.ky / 2, KXY, g.nxh, g.kplanes, a.y, t.y_cols_log2, t.threads, st));
+            d_cols_kx(KX, g.pitch, g.krows, g.ky / 2, KXY, g.nxh, g.kplanes, a.y, t.y_cols_log2, t.threads, st));
   } else {
     const long long rows = (long long)g.ny * g.nz;
     FC_PASS("kernel_x_r2c", 4.0 * g.nx * rows + 8.0 * g.nxh * rows, st,
-            launch_x_r2c_dense(d_kernel, g.nx, KXY, g.pitch, rows, a.x, t, st));
+            d_x_r2c_dense(d_kernel, g.nx, KXY, g.pitch, rows, a.x, t, st));
     FC_PASS("kernel_y_fwd", 16.0 * g.nxh * rows, st,
-            launch_cols(KXY, KXY, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2,
+            d_cols(KXY, KXY, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2,
                         t.threads, st));
   }
   (void)row;
@@ -354,9 +403,9 @@ static void enqueue_kernel_spectrum(const Geom& g, const Axes& a, const Tiles& t
 static void enqueue_xy_fwd(const Geom& g, const Axes& a, const Tiles& t, const float* d_in, float2* S,
                            cudaStream_t st, const char* xname, const char* yname) {
   const long long rows = (long long)g.ny * g.nz;
-  FC_PASS(xname, 4.0 * g.N() + 8.0 * g.nxh * rows, st, launch_x_r2c_dense(d_in, g.nx, S, g.pitch, rows, a.x, t, st));
+  FC_PASS(xname, 4.0 * g.N() + 8.0 * g.nxh * rows, st, d_x_r2c_dense(d_in, g.nx, S, g.pitch, rows, a.x, t, st));
   FC_PASS(yname, 16.0 * g.nxh * rows, st,
-          launch_cols(S, S, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2, t.threads,
+          d_cols(S, S, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2, t.threads,
                       st));
 }
 
@@ -364,9 +413,9 @@ static void enqueue_yx_inv(const Geom& g, const Axes& a, const Tiles& t, float2*
                            const char* yname, const char* xname) {
   const long long rows = (long long)g.ny * g.nz;
   FC_PASS(yname, 16.0 * g.nxh * rows, st,
-          launch_cols(S, S, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, true, a.y, t.y_cols_log2, t.threads,
+          d_cols(S, S, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, true, a.y, t.y_cols_log2, t.threads,
                       st));
-  FC_PASS(xname, 4.0 * g.N() + 8.0 * g.nxh * rows, st, launch_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
+  FC_PASS(xname, 4.0 * g.N() + 8.0 * g.nxh * rows, st, d_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
 }
 
 
@@ -398,7 +447,7 @@ static void enqueue_conv(DevCtx& c, const Geom& g0, const float* d_image, float*
   enqueue_xy_fwd(g, a, t, d_image, S, st, "image_x_r2c", "image_y_fwd");
   const double mcy = 8.0 * g.nxh * (double)g.ny * g.nz;
   FC_PASS("zconv", 2.0 * mcy + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
-          launch_zconv(S, (const float2*)(ws + L.off_KXY), g.pitch, g.ny, g.nxh, g.kplanes, g.kbox ? g.kz / 2 : 0,
+          d_zconv(S, (const float2*)(ws + L.off_KXY), g.pitch, g.ny, g.nxh, g.kplanes, g.kbox ? g.kz / 2 : 0,
                        1.0f / (float)g.N(), false, a.z, t.z_cols_log2, t.threads, st));
   enqueue_yx_inv(g, a, t, S, d_out, st, "image_y_inv", "image_x_c2r");
 }
@@ -446,7 +495,7 @@ static void enqueue_adjoint(DevCtx& c, const Geom& g, const float* d_x, const fl
   if (d_gk) {
     enqueue_xy_fwd(g, a, t, d_x, SX, st, "image_x_r2c", "image_y_fwd");
     FC_PASS("zcorr_crop", 16.0 * g.nxh * (double)g.ny * g.nz + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
-            launch_zcorr_crop(SX, SG, GK, g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, a.z, t.z_cols_log2, t.threads,
+            d_zcorr(SX, SG, GK, g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, a.z, t.z_cols_log2, t.threads,
                               st));
   }
   if (d_gx) {
@@ -455,18 +504,18 @@ static void enqueue_adjoint(DevCtx& c, const Geom& g, const float* d_x, const fl
     kl.off_KXY = L.off_KXY;
     enqueue_kernel_spectrum(g, a, t, d_k, ws, kl, st);
     FC_PASS("zconv_conj", 16.0 * g.nxh * (double)g.ny * g.nz + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
-            launch_zconv(SG, (const float2*)(ws + L.off_KXY), g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, true, a.z,
+            d_zconv(SG, (const float2*)(ws + L.off_KXY), g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, true, a.z,
                          t.z_cols_log2, t.threads, st));
     enqueue_yx_inv(g, a, t, SG, d_gx, st, "grad_image_y_inv", "grad_image_x_c2r");
   }
   if (d_gk) {
     const long long rows = (long long)g.ny * g.kplanes;
     FC_PASS("grad_kernel_y_inv", 16.0 * g.nxh * rows, st,
-            launch_cols(GK, GK, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.kplanes, true, a.y, t.y_cols_log2,
+            d_cols(GK, GK, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.kplanes, true, a.y, t.y_cols_log2,
                         t.threads, st));
     float* dst = g.kbox ? GKR : d_gk;
     FC_PASS("grad_kernel_x_c2r", 8.0 * g.nxh * rows + 4.0 * g.nx * rows, st,
-            launch_x_c2r(GK, g.pitch, dst, g.nx, rows, a.x, t, st));
+            d_x_c2r(GK, g.pitch, dst, g.nx, rows, a.x, t, st));
     if (g.kbox)
       FC_PASS("grad_kernel_crop", 8.0 * g.kx * g.ky * g.kz, st,
               launch_crop_kernel(GKR, g.nx, g.ny, g.nx, g.kx, g.ky, g.kz, d_gk, st));
@@ -486,7 +535,7 @@ static void enqueue_rfft3d(DevCtx& c, const Geom& g, const float* d_in, float* d
   // z pass as a column pass over planes of constant y; the result is written
   // into the caller's dense layout (pitch nxh) by a final strided z pass
   FC_PASS("fft_z_fwd", 16.0 * g.nxh * (double)g.ny * g.nz, st,
-          launch_cols(S, S, g.pitch, (long long)g.ny * g.pitch, g.nxh, g.ny, false, a.z, t.z_cols_log2, t.threads,
+          d_cols(S, S, g.pitch, (long long)g.ny * g.pitch, g.nxh, g.ny, false, a.z, t.z_cols_log2, t.threads,
                       st));
   cuda_check(cudaMemcpy2DAsync(d_spec, sizeof(float2) * g.nxh, S, sizeof(float2) * g.pitch, sizeof(float2) * g.nxh,
                                (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, st),
@@ -503,7 +552,7 @@ static void enqueue_irfft3d(DevCtx& c, const Geom& g, const float* d_spec, float
                                (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, st),
              "cudaMemcpy2DAsync");
   FC_PASS("fft_z_inv", 16.0 * g.nxh * (double)g.ny * g.nz, st,
-          launch_cols(S, S, g.pitch, (long long)g.ny * g.pitch, g.nxh, g.ny, true, a.z, t.z_cols_log2, t.threads, st));
+          d_cols(S, S, g.pitch, (long long)g.ny * g.pitch, g.nxh, g.ny, true, a.z, t.z_cols_log2, t.threads, st));
   enqueue_yx_inv(g, a, t, S, d_out, st, "fft_y_inv", "fft_x_c2r");
 }
 
@@ -587,6 +636,7 @@ int fc_last_status(void) { return t_status; }
 const char* fc_last_error(void) { return t_error.c_str(); }
 void fc_free_result(imageType* p) { delete[] p; }
 void fc_set_shift_compat(int on) { g_shift_compat = on ? 1 : 0; }
+void fc_set_generic_kernels(int on) { g_generic_only = on ? 1 : 0; }
 const char* fc_version(void) { return "fc-gb300 0.1.0 (sm_103a)"; }
 int fc_launch_count(void) { return t_launches; }
 

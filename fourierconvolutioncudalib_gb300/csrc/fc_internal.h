@@ -74,6 +74,26 @@ cudaError_t launch_pad_shift(const float* taps, int kx, int ky, int kz, int nx, 
 cudaError_t launch_crop_kernel(const float* vol, long long row_pitch, int ny_rows, int nx, int kx, int ky, int kz,
                                float* out, cudaStream_t st);
 
+// Register-resident fast path for power-of-two lengths (fc_fast_rows.cu,
+// fc_fast_cols.cu).  Same contracts as the generic launchers above; they
+// return cudaErrorNotSupported for lengths they do not cover.
+bool fast_rows_supported(int n);
+bool fast_cols_supported(int n);
+cudaError_t fast_x_r2c_dense(const float* in, long long in_pitch, float2* out, long long out_pitch, long long nrows,
+                             const FcAxis& ax, cudaStream_t st);
+cudaError_t fast_x_r2c_box(const float* taps, int kx, int hx, float2* out, long long out_pitch, long long nrows,
+                           const FcAxis& ax, cudaStream_t st);
+cudaError_t fast_x_c2r(const float2* in, long long in_pitch, float* out, long long out_pitch, long long nrows,
+                       const FcAxis& ax, cudaStream_t st);
+cudaError_t fast_cols(const float2* src, float2* dst, long long ps, long long es, int ncols, int nplanes, bool inverse,
+                      const FcAxis& ax, cudaStream_t st);
+cudaError_t fast_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
+                         int nplanes, const FcAxis& ax, cudaStream_t st);
+cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+                       float scale, bool conj_kernel, const FcAxis& az, cudaStream_t st);
+cudaError_t fast_zcorr(const float2* X, const float2* G, float2* out, long long pitch, int ny, int ncols, int kz,
+                       int hz, float scale, const FcAxis& az, cudaStream_t st);
+
 // reference thread-count helper (src/convolution3Dfft.cu:26-38) restated for
 // the compat scatter's grid truncation
 int ref_closest_multiplier(int a_number, int multiplier);

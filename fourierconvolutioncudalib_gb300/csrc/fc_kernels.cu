@@ -14,25 +14,9 @@
 // pass: only the rows and planes that hold taps are transformed.
 #include "fc_internal.h"
 #include "fc_fft.cuh"
+#include "fc_sources.cuh"
 
 namespace fc {
-
-// ------------------------------------------------------------------ sources
-struct SrcDense {  // real rows of a dense volume
-  const float* p;
-  long long pitch;
-  __device__ __forceinline__ float load(long long row, int x) const { return __ldg(p + row * pitch + x); }
-};
-
-struct SrcBox {  // kernel taps [kz][ky][kx]; row = plane*ky + iy; x -> ix = (x + hx) mod nx
-  const float* k;
-  int kx, hx, nx;
-  __device__ __forceinline__ float load(long long row, int x) const {
-    int ix = x + hx;
-    if (ix >= nx) ix -= nx;
-    return ix < kx ? __ldg(k + row * kx + ix) : 0.f;
-  }
-};
 
 // ------------------------------------------------------------------ x pass, R2C
 // CTA: 2P real rows -> P complex lines z = a + i b -> FFT -> split into the two
@@ -124,26 +108,6 @@ __global__ void __launch_bounds__(256) k_x_c2r(const float2* __restrict__ in, lo
     }
   }
 }
-
-// ------------------------------------------------------------------ column passes
-struct ColPlain {
-  const float2* p;
-  long long ps, es;
-  __device__ __forceinline__ float2 load(int plane, int j, int c) const {
-    return p[(long long)plane * ps + (long long)j * es + c];
-  }
-};
-
-struct ColKX {  // compact kernel x-spectrum rows: plane*krows + iy, y -> iy = (y + hy) mod ny
-  const float2* p;
-  long long pitch;
-  int krows, hy, ny;
-  __device__ __forceinline__ float2 load(int plane, int y, int c) const {
-    int iy = y + hy;
-    if (iy >= ny) iy -= ny;
-    return iy < krows ? p[((long long)plane * krows + iy) * pitch + c] : make_float2(0.f, 0.f);
-  }
-};
 
 template <bool INV, class Src>
 __global__ void __launch_bounds__(256) k_cols(Src src, float2* dst, long long ps, long long es, int ncols,

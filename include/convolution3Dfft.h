@@ -102,6 +102,10 @@ FUNCTION_PREFIX void fc_free_result(imageType* p);
    0 = centred circular shift (default), 1 = reference InPlace arithmetic.  The
    environment variable FC_SHIFT_COMPAT=1 sets 1 at load time. */
 FUNCTION_PREFIX void fc_set_shift_compat(int on);
+/* kernel selection: 0 = register-resident kernels for power-of-two axes and
+   the generic shared-memory kernels elsewhere (default); 1 = generic kernels
+   on every axis.  The environment variable FC_GENERIC=1 sets 1 at load time. */
+FUNCTION_PREFIX void fc_set_generic_kernels(int on);
 /* free the cached workspace, staging buffers and plans held for a device */
 FUNCTION_PREFIX int fc_release_device(int devCUDA);
 /* library version, e.g. "fc-gb300 0.1.0 (sm_103a)" */

@@ -19,12 +19,19 @@ SHAPES = [  # (z, y, x)
     (7, 49, 343),   # power_of_7 (:353-384)
     (128, 128, 128),  # cube_128_shape (:386-416)
     (7, 14, 343),   # out-of-place variant shape
-    (128, 512, 512), (96, 448, 384), (1, 1, 64), (2, 3, 4), (1, 1, 1),
+    (128, 512, 512), (96, 448, 384), (1, 1, 64), (2, 3, 4), (1, 1, 1), (8, 16, 4096), (4, 1024, 32),
 ]
 
 
+@pytest.fixture(params=["fast", "generic"])
+def kernels(request, fclib):
+    fclib.fc_set_generic_kernels(1 if request.param == "generic" else 0)
+    yield request.param
+    fclib.fc_set_generic_kernels(0)
+
+
 @pytest.mark.parametrize("shape", SHAPES)
-def test_rfft3d_and_round_trip(cuda, shape):
+def test_rfft3d_and_round_trip(cuda, kernels, shape):
     import torch
     from fourierconvolutioncudalib_gb300 import device as fcd
     from oracle import oracle as orc

@@ -18,6 +18,15 @@ MAXABS_TOL = 1e-5
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["fast", "generic"])
+def kernels(request, fclib):
+    """Run a test on the register-resident kernels (power-of-two axes) and on
+    the generic shared-memory kernels (forced on every axis)."""
+    fclib.fc_set_generic_kernels(1 if request.param == "generic" else 0)
+    yield request.param
+    fclib.fc_set_generic_kernels(0)
+
+
 def _check(out, ref, rel=REL_TOL, mx=MAXABS_TOL):
     from oracle import oracle as orc
 
@@ -35,7 +44,7 @@ def _gauss(k, s):
     return (g / g.sum()).astype(np.float32)
 
 
-def test_c1_plain_small_vs_fp64(cuda, orc):
+def test_c1_plain_small_vs_fp64(cuda, orc, kernels):
     # 64^3 uniform[0,1) (seed 1), 7^3 isotropic Gaussian sigma 1.5 normalised
     rng = np.random.Generator(np.random.PCG64(1))
     im = rng.random((64, 64, 64)).astype(np.float32)
@@ -48,7 +57,7 @@ def test_c1_plain_small_vs_fp64(cuda, orc):
     _check(out, orc.conv_fp64(im, k, "reference_inplace"))
 
 
-def test_c1_vs_cufft_sequence(cuda, orc):
+def test_c1_vs_cufft_sequence(cuda, orc, kernels):
     from baseline import refseq
 
     rng = np.random.Generator(np.random.PCG64(1))
@@ -71,8 +80,12 @@ def test_c1_vs_cufft_sequence(cuda, orc):
     ((1, 64, 64), (1, 5, 5)),         # a 2D image as a 1-plane volume
     ((22, 26, 34), (11, 13, 17)),     # radix 11 and 13 and a generic prime (17)
     ((37, 79, 109), (5, 5, 5)),       # large primes from the padded reference KAT extents
+    ((128, 512, 512), (63, 31, 31)),  # the microscope configuration's shapes
+    ((64, 256, 1024), (9, 9, 9)),     # 1024 rows
+    ((16, 2048, 128), (3, 5, 3)),     # a 2048 column axis (generic kernels)
+    ((256, 64, 32), (5, 3, 3)),       # short rows, long z
 ])
-def test_shapes_vs_fp64(cuda, orc, shape, kshape):
+def test_shapes_vs_fp64(cuda, orc, kernels, shape, kshape):
     rng = np.random.default_rng(sum(shape) + sum(kshape))
     im = rng.random(shape, dtype=np.float32)
     k = rng.random(kshape, dtype=np.float32)
@@ -85,7 +98,7 @@ def test_shapes_vs_fp64(cuda, orc, shape, kshape):
     _check(out, ref)
 
 
-def test_reference_kats(cuda, orc):
+def test_reference_kats(cuda, orc, kernels):
     """Every convolution known-answer case of the reference test suite, through
     convolution3DfftCUDAInPlace with the reference's padding protocol."""
     for case in orc.kat_cases(include_large=True):
@@ -111,7 +124,7 @@ def test_reference_kats(cuda, orc):
             assert orc.l2norm(re, got) < case["threshold"], case["name"]
 
 
-def test_shift_compat_matches_reference_arithmetic(cuda, orc):
+def test_shift_compat_matches_reference_arithmetic(cuda, orc, kernels):
     """With the reference's placement arithmetic the result equals the FP64
     oracle of that (scrambled) placement on non-cubic shapes."""
     rng = np.random.default_rng(7)
@@ -146,7 +159,7 @@ def test_padded_kernel_bit_exact(cuda, orc):
         assert np.array_equal(got_d.view(np.uint32), orc.centered_padded_kernel(k, shape).view(np.uint32))
 
 
-def test_non_inplace_entries(cuda, orc):
+def test_non_inplace_entries(cuda, orc, kernels):
     rng = np.random.default_rng(11)
     im = rng.random((20, 24, 18), dtype=np.float32)   # dims slowest-first (d0,d1,d2)
     k = rng.random((5, 3, 7), dtype=np.float32)
