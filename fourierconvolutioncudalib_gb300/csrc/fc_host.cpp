@@ -376,27 +376,74 @@ static Axes axes_for(DevCtx& c, const Geom& g) {
   return a;
 }
 
-// kernel spectrum KXY from taps (box) or a dense N-float kernel
-static void enqueue_kernel_spectrum(const Geom& g, const Axes& a, const Tiles& t, const float* d_kernel, char* ws,
-                                    const Layout& L, cudaStream_t st) {
-  float2* KX = (float2*)(ws + L.off_KX);
-  float2* KXY = (float2*)(ws + L.off_KXY);
-  const double row = (double)g.pitch * 8.0;
+// kernel spectrum: x pass of the taps (box) or of the dense kernel
+static void enqueue_kernel_x(const Geom& g, const Axes& a, const Tiles& t, const float* d_kernel, char* ws,
+                             const Layout& L, cudaStream_t st) {
   if (g.kbox) {
     const long long rows = (long long)g.kplanes * g.krows;
     FC_PASS("kernel_x_r2c", 4.0 * g.kx * rows + 8.0 * g.nxh * rows, st,
-            d_x_r2c_box(d_kernel, g.kx, g.kx / 2, KX, g.pitch, rows, a.x, t, st));
-    FC_PASS("kernel_y_fwd", 8.0 * g.nxh * (rows + (double)g.ny * g.kplanes), st,
-            d_cols_kx(KX, g.pitch, g.krows, g.ky / 2, KXY, g.nxh, g.kplanes, a.y, t.y_cols_log2, t.threads, st));
+            d_x_r2c_box(d_kernel, g.kx, g.kx / 2, (float2*)(ws + L.off_KX), g.pitch, rows, a.x, t, st));
   } else {
     const long long rows = (long long)g.ny * g.nz;
     FC_PASS("kernel_x_r2c", 4.0 * g.nx * rows + 8.0 * g.nxh * rows, st,
-            d_x_r2c_dense(d_kernel, g.nx, KXY, g.pitch, rows, a.x, t, st));
-    FC_PASS("kernel_y_fwd", 16.0 * g.nxh * rows, st,
-            d_cols(KXY, KXY, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2,
-                        t.threads, st));
+            d_x_r2c_dense(d_kernel, g.nx, (float2*)(ws + L.off_KXY), g.pitch, rows, a.x, t, st));
   }
-  (void)row;
+}
+
+// kernel spectrum: y pass over spectrum columns [c0, c0 + w)
+static void enqueue_kernel_y(const Geom& g, const Axes& a, const Tiles& t, char* ws, const Layout& L, int c0, int w,
+                             cudaStream_t st) {
+  float2* KXY = (float2*)(ws + L.off_KXY) + c0;
+  if (g.kbox) {
+    const double rows = (double)g.kplanes * g.krows;
+    FC_PASS("kernel_y_fwd", 8.0 * w * (rows + (double)g.ny * g.kplanes), st,
+            d_cols_kx((float2*)(ws + L.off_KX) + c0, g.pitch, g.krows, g.ky / 2, KXY, w, g.kplanes, a.y,
+                      t.y_cols_log2, t.threads, st));
+  } else {
+    FC_PASS("kernel_y_fwd", 16.0 * w * (double)g.ny * g.nz, st,
+            d_cols(KXY, KXY, (long long)g.ny * g.pitch, g.pitch, w, g.nz, false, a.y, t.y_cols_log2, t.threads, st));
+  }
+}
+
+// kernel spectrum for all columns (used where no chunking applies)
+static void enqueue_kernel_spectrum(const Geom& g, const Axes& a, const Tiles& t, const float* d_kernel, char* ws,
+                                    const Layout& L, cudaStream_t st) {
+  enqueue_kernel_x(g, a, t, d_kernel, ws, L, st);
+  enqueue_kernel_y(g, a, t, ws, L, 0, g.nxh, st);
+}
+
+// Spectrum columns per L2 chunk.  The y-forward, fused z and y-inverse
+// passes (and the kernel's y pass) can run chunk by chunk over kx, each chunk
+// sized so that its image and kernel spectra fit in a budget of L2 bytes, so
+// that a chunk's intermediate results could be re-read from L2 rather than
+// HBM.  Measured on GB300 at 512x512x128 this is slower than one launch per
+// pass at every budget from 24 to 96 MB (smaller grids, shorter row segments,
+// no visible L2 reuse), so it is off unless asked for: FC_L2_CHUNK_MB or
+// fc_set_l2_chunk_bytes (-1 = half the device's L2).
+static long long g_l2_chunk_bytes = -2;  // -2: read env (default 0 = off)
+static int chunk_cols(const Geom& g) {
+  if (g_l2_chunk_bytes == -2) {
+    const char* e = std::getenv("FC_L2_CHUNK_MB");
+    g_l2_chunk_bytes = e ? (long long)(std::atof(e) * 1048576.0) : 0;
+  }
+  long long budget = g_l2_chunk_bytes;
+  if (budget < 0) {
+    int dev = 0, l2 = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) {
+      cudaGetLastError();
+      l2 = 0;
+    }
+    budget = (long long)l2 / 2;
+  }
+  if (budget <= 0) return g.nxh;
+  const long long per_col = 8LL * g.ny * (g.nz + g.kplanes);
+  long long cw = budget / per_col;
+  if (cw >= g.nxh) return g.nxh;
+  if (cw < 16) cw = 16;
+  const long long n = (g.nxh + cw - 1) / cw;
+  cw = ((g.nxh + n - 1) / n + 7) / 8 * 8;
+  return (int)std::min<long long>(cw, g.nxh);
 }
 
 // forward x and y passes of a real volume into spectrum S
@@ -443,13 +490,24 @@ static void enqueue_conv(DevCtx& c, const Geom& g0, const float* d_image, float*
   const Tiles t = choose_tiles(g);
   const Axes a = axes_for(c, g);
   float2* S = (float2*)(ws + L.off_S);
-  enqueue_kernel_spectrum(g, a, t, ksrc, ws, L, st);
-  enqueue_xy_fwd(g, a, t, d_image, S, st, "image_x_r2c", "image_y_fwd");
-  const double mcy = 8.0 * g.nxh * (double)g.ny * g.nz;
-  FC_PASS("zconv", 2.0 * mcy + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
-          d_zconv(S, (const float2*)(ws + L.off_KXY), g.pitch, g.ny, g.nxh, g.kplanes, g.kbox ? g.kz / 2 : 0,
-                       1.0f / (float)g.N(), false, a.z, t.z_cols_log2, t.threads, st));
-  enqueue_yx_inv(g, a, t, S, d_out, st, "image_y_inv", "image_x_c2r");
+  const long long rows = (long long)g.ny * g.nz;
+  const long long ps = (long long)g.ny * g.pitch;
+  enqueue_kernel_x(g, a, t, ksrc, ws, L, st);
+  FC_PASS("image_x_r2c", 4.0 * g.N() + 8.0 * g.nxh * rows, st,
+          d_x_r2c_dense(d_image, g.nx, S, g.pitch, rows, a.x, t, st));
+  const int cw = chunk_cols(g);
+  for (int c0 = 0; c0 < g.nxh; c0 += cw) {
+    const int w = std::min(cw, g.nxh - c0);
+    enqueue_kernel_y(g, a, t, ws, L, c0, w, st);
+    FC_PASS("image_y_fwd", 16.0 * w * (double)rows, st,
+            d_cols(S + c0, S + c0, ps, g.pitch, w, g.nz, false, a.y, t.y_cols_log2, t.threads, st));
+    FC_PASS("zconv", 16.0 * w * (double)rows + 8.0 * w * (double)g.ny * g.kplanes, st,
+            d_zconv(S + c0, (const float2*)(ws + L.off_KXY) + c0, g.pitch, g.ny, w, g.kplanes,
+                    g.kbox ? g.kz / 2 : 0, 1.0f / (float)g.N(), false, a.z, t.z_cols_log2, t.threads, st));
+    FC_PASS("image_y_inv", 16.0 * w * (double)rows, st,
+            d_cols(S + c0, S + c0, ps, g.pitch, w, g.nz, true, a.y, t.y_cols_log2, t.threads, st));
+  }
+  FC_PASS("image_x_c2r", 4.0 * g.N() + 8.0 * g.nxh * rows, st, d_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
 }
 
 // ------------------------------------------------------------------ adjoint
@@ -637,6 +695,7 @@ const char* fc_last_error(void) { return t_error.c_str(); }
 void fc_free_result(imageType* p) { delete[] p; }
 void fc_set_shift_compat(int on) { g_shift_compat = on ? 1 : 0; }
 void fc_set_generic_kernels(int on) { g_generic_only = on ? 1 : 0; }
+void fc_set_l2_chunk_bytes(long long bytes) { g_l2_chunk_bytes = bytes < 0 ? -1 : bytes; }
 const char* fc_version(void) { return "fc-gb300 0.1.0 (sm_103a)"; }
 int fc_launch_count(void) { return t_launches; }
 

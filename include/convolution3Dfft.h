@@ -106,6 +106,10 @@ FUNCTION_PREFIX void fc_set_shift_compat(int on);
    the generic shared-memory kernels elsewhere (default); 1 = generic kernels
    on every axis.  The environment variable FC_GENERIC=1 sets 1 at load time. */
 FUNCTION_PREFIX void fc_set_generic_kernels(int on);
+/* L2 budget of one column chunk of the y / fused-z / y-inverse passes:
+   0 = no chunking (default), -1 = half the device L2, else bytes.  The
+   environment variable FC_L2_CHUNK_MB sets it at load time. */
+FUNCTION_PREFIX void fc_set_l2_chunk_bytes(long long bytes);
 /* free the cached workspace, staging buffers and plans held for a device */
 FUNCTION_PREFIX int fc_release_device(int devCUDA);
 /* library version, e.g. "fc-gb300 0.1.0 (sm_103a)" */

@@ -198,3 +198,21 @@ def test_device_queries(cuda):
     assert fc.getMemDeviceCUDA(d) > (1 << 30)
     assert fc.cuda_version() >= 13000
     assert fc.gpu_mem_needed_mb([128, 512, 512]) > 0
+
+
+@pytest.mark.parametrize("chunk_bytes", [0, 3 << 20, 17 << 20, -1])
+def test_l2_column_chunks_equivalent(cuda, orc, kernels, chunk_bytes):
+    """The y / fused-z / y-inverse passes run over kx column chunks sized for
+    L2; every chunking gives the same result as none (and the oracle's)."""
+    rng = np.random.default_rng(21)
+    im = rng.random((32, 96, 200), dtype=np.float32)
+    k = rng.random((7, 5, 9), dtype=np.float32)
+    k /= k.sum()
+    ref = orc.conv_fp64(im, k, "centered")
+    out = im.copy()
+    fc.lib().fc_set_l2_chunk_bytes(chunk_bytes)
+    try:
+        fc.convolution3DfftCUDAInPlace(out, (200, 96, 32), k, (9, 5, 7), 0)
+    finally:
+        fc.lib().fc_set_l2_chunk_bytes(0)
+    _check(out, ref)
