@@ -93,6 +93,7 @@ _SIGNATURES = {
     "fc_profile_enable": (None, [_I]),
     "fc_profile_read": (_I, [ctypes.c_char_p, _I, _FP, ctypes.POINTER(ctypes.c_double), _I]),
     "fc_launch_count": (_I, []),
+    "fc_conv3d_device_noalloc": (_I, [_P, _P, _IP, _P, _IP, _I, _P]),
 }
 
 

@@ -23,7 +23,7 @@ LIB_PATH = PKG / LIB_NAME
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", str(ROOT / "include")]
-SOURCES = ["fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu"]
+SOURCES = ["fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu", "fc_noalloc.cu"]
 
 
 def nvcc() -> str:

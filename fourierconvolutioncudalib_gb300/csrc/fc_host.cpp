@@ -32,6 +32,7 @@ namespace fc {
 static thread_local int t_status = FC_OK;
 static thread_local std::string t_error;
 static thread_local int t_launches = 0;
+static thread_local bool t_no_events = false;  // set while enqueuing for the allocation-free entry point
 
 struct FcError {
   int code;
@@ -291,7 +292,7 @@ struct PassScope {
   const char* name;
   double bytes;
   cudaStream_t st;
-  PassScope(const char* nm, double by, cudaStream_t s) : on(g_prof_on), name(nm), bytes(by), st(s) {
+  PassScope(const char* nm, double by, cudaStream_t s) : on(g_prof_on && !t_no_events), name(nm), bytes(by), st(s) {
     if (on) {
       cudaEventCreate(&a);
       cudaEventCreate(&b);
@@ -474,8 +475,19 @@ static Geom effective_geom(const Geom& g, bool compat) {
 static Layout plain_layout(const Geom& g, bool compat) { return conv_layout(effective_geom(g, compat), compat && g.kbox); }
 
 // Enqueue a full convolution.  d_kernel: taps (box) or dense N floats.
+static void enqueue_conv_core(const Geom& g0, const Axes& a, const float* d_image, float* d_out,
+                              const float* d_kernel, bool compat, char* ws, size_t ws_bytes, cudaStream_t st);
+
 static void enqueue_conv(DevCtx& c, const Geom& g0, const float* d_image, float* d_out, const float* d_kernel,
                          bool compat, char* ws, size_t ws_bytes, cudaStream_t st) {
+  enqueue_conv_core(g0, axes_for(c, g0), d_image, d_out, d_kernel, compat, ws, ws_bytes, st);
+}
+
+// The pass sequence of one convolution, with the twiddle tables given by the
+// caller (a.x.W, a.y.W, a.z.W): enqueues kernels and one memset, allocates
+// nothing and creates no CUDA object (profiling events aside).
+static void enqueue_conv_core(const Geom& g0, const Axes& a, const float* d_image, float* d_out,
+                              const float* d_kernel, bool compat, char* ws, size_t ws_bytes, cudaStream_t st) {
   const Geom g = effective_geom(g0, compat);
   const Layout L = conv_layout(g, compat && g0.kbox);
   if (ws_bytes < L.total) FC_THROW(FC_ERR_NOMEM, "workspace too small");
@@ -488,7 +500,6 @@ static void enqueue_conv(DevCtx& c, const Geom& g0, const float* d_image, float*
     ksrc = dense;
   }
   const Tiles t = choose_tiles(g);
-  const Axes a = axes_for(c, g);
   float2* S = (float2*)(ws + L.off_S);
   const long long rows = (long long)g.ny * g.nz;
   const long long ps = (long long)g.ny * g.pitch;
@@ -681,6 +692,56 @@ static void dims3(const int* d, int* a, int* b, int* cc) {
   *a = d[0];
   *b = d[1];
   *cc = d[2];
+}
+
+// ------------------------------------------------------------------ scratch-only convolution
+// Used by the allocation-free entry point (fc_noalloc.cu).  Layout of the
+// scratch: the three twiddle tables, then the convolution workspace.
+void record_status(int code, const char* msg) { set_status(code, msg ? msg : ""); }
+
+int conv_in_scratch(const float* d_image, float* d_out, const int* imDim, const float* d_kernel,
+                    const int* kernelDim, int flags, char* scratch, size_t scratch_bytes, cudaStream_t st) {
+  clear_status();
+  return guarded([&] {
+    if (!d_image || !d_out || !d_kernel || !scratch) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    if (flags & (FC_FLAG_TC_FP16 | FC_FLAG_TC_BF16))
+      FC_THROW(FC_ERR_UNSUPPORTED, "the allocation-free entry point runs the fp32 path only");
+    int nx, ny, nz, kx = 0, ky = 0, kz = 0;
+    dims3(imDim, &nx, &ny, &nz);
+    const bool dense = flags & FC_FLAG_DENSE_KERNEL;
+    if (!dense) dims3(kernelDim, &kx, &ky, &kz);
+    const Geom g = make_geom(nx, ny, nz, kx, ky, kz, dense);
+    const bool compat = (flags & FC_FLAG_SHIFT_COMPAT) && g.kbox;
+    const size_t tw = align256(sizeof(float2) * ((size_t)nx + ny + nz));
+    const size_t need = tw + plain_layout(g, compat).total;
+    if (need > scratch_bytes)
+      FC_THROW(FC_ERR_NOMEM, "this convolution needs " + std::to_string(need) + " bytes of scratch; the static scratch "
+                             "of the allocation-free entry point holds " + std::to_string(scratch_bytes));
+    float2* W = (float2*)scratch;
+    Axes a;
+    const int n3[3] = {nx, ny, nz};
+    FcAxis* ax3[3] = {&a.x, &a.y, &a.z};
+    size_t off = 0;
+    for (int i = 0; i < 3; ++i) {
+      FcAxis& ax = *ax3[i];
+      std::memset(&ax, 0, sizeof(ax));
+      ax.n = n3[i];
+      int r[FC_MAX_STAGES];
+      const int ns = plan_radices(n3[i], r, FC_MAX_STAGES);
+      if (ns < 0) FC_THROW(FC_ERR_UNSUPPORTED, "no radix plan for length " + std::to_string(n3[i]));
+      ax.nst = (n3[i] == 1) ? 0 : ns;
+      for (int k = 0; k < ns; ++k) ax.radix[k] = r[k];
+      ax.W = W + off;
+      cuda_check(launch_make_twiddles(W + off, n3[i], st), "twiddles");
+      ++t_launches;
+      off += (size_t)n3[i];
+    }
+    struct NoEvents {
+      NoEvents() { t_no_events = true; }
+      ~NoEvents() { t_no_events = false; }
+    } no_events;
+    enqueue_conv_core(g, a, d_image, d_out, d_kernel, compat, scratch + tw, scratch_bytes - tw, st);
+  });
 }
 
 }  // namespace fc

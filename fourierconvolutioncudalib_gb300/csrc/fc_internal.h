@@ -94,6 +94,17 @@ cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, in
 cudaError_t fast_zcorr(const float2* X, const float2* G, float2* out, long long pitch, int ny, int ncols, int kz,
                        int hz, float scale, const FcAxis& az, cudaStream_t st);
 
+// W[k] = exp(-2 pi i k / n) computed on the device (double precision, rounded once)
+cudaError_t launch_make_twiddles(float2* W, int n, cudaStream_t st);
+
+// Plain convolution (fc_conv3d_device semantics) whose twiddle tables and
+// workspace are carved out of caller-owned device scratch; allocates nothing.
+// Sets the thread's status and returns it.
+int conv_in_scratch(const float* d_image, float* d_out, const int* imDim, const float* d_kernel,
+                    const int* kernelDim, int flags, char* scratch, size_t scratch_bytes, cudaStream_t st);
+// record a failure of the caller's own set-up in the thread's status
+void record_status(int code, const char* msg);
+
 // reference thread-count helper (src/convolution3Dfft.cu:26-38) restated for
 // the compat scatter's grid truncation
 int ref_closest_multiplier(int a_number, int multiplier);

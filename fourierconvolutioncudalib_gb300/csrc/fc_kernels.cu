@@ -284,6 +284,18 @@ __global__ void k_crop_kernel(const float* __restrict__ vol, long long row_pitch
   }
 }
 
+// ------------------------------------------------------------------ twiddles on the device
+// W[k] = exp(-2 pi i k / n) evaluated in double precision (sincospi of the
+// exact-as-possible ratio -2k/n) and rounded once to float: the device-side
+// twin of the host table, for callers whose twiddles live in static memory.
+__global__ void k_make_twiddles(float2* __restrict__ W, int n) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    double sn, cs;
+    sincospi(-2.0 * (double)k / (double)n, &sn, &cs);
+    W[k] = make_float2((float)cs, (float)sn);
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 static inline size_t row_smem(int n, int pairs_log2) { return (size_t)2 * (1 << pairs_log2) * (n | 1) * sizeof(float2); }
 
@@ -430,6 +442,12 @@ cudaError_t launch_crop_kernel(const float* vol, long long row_pitch, int ny_row
   if (K <= 0) return cudaSuccess;
   const unsigned grid = (unsigned)((K + 255) / 256 < 65535 ? (K + 255) / 256 : 65535);
   k_crop_kernel<<<grid, 256, 0, st>>>(vol, row_pitch, ny_rows, nx, kx, ky, kz, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_make_twiddles(float2* W, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_make_twiddles<<<(n + 255) / 256, 256, 0, st>>>(W, n);
   return cudaGetLastError();
 }
 

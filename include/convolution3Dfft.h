@@ -174,4 +174,23 @@ FUNCTION_PREFIX int fc_profile_read(char* names, int name_stride, float* ms, dou
 /* number of kernel launches the most recent fc_* / reference call made */
 FUNCTION_PREFIX int fc_launch_count(void);
 
+/* Allocation-free variant of fc_conv3d_device (no counterpart in the
+ * reference).  For callers that cannot allocate device memory when they
+ * convolve -- a framework that has reserved the GPU's memory in its own pool,
+ * a real-time loop that cannot take cudaMalloc's implicit synchronisation, a
+ * deployment that forbids device allocation after start-up.  Same arguments
+ * and result as fc_conv3d_device (fp32 path, FC_FLAG_SHIFT_COMPAT and
+ * FC_FLAG_DENSE_KERNEL honoured) but no workspace argument: all scratch,
+ * including the twiddle tables, comes from one static device array of
+ * FC_NOALLOC_SCRATCH_BYTES per device, held by every process that loads the
+ * library until it exits.  A convolution needing more scratch than that is
+ * rejected with FC_ERR_NOMEM and a message giving both sizes (e.g. a
+ * 256x256x128 image with a 31x31x63 kernel needs about 56 MiB).  The first
+ * call on a device looks up the array's device address, so make it before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+#define FC_NOALLOC_SCRATCH_BYTES (64ull << 20)
+FUNCTION_PREFIX int fc_conv3d_device_noalloc(const float* d_image, float* d_out, const int* imDim,
+                                             const float* d_kernel, const int* kernelDim, int flags, void* stream);
+
 #endif /* FC_GB300_CONVOLUTION_3D_FFT_H */
