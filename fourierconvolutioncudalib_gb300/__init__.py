@@ -75,6 +75,7 @@ _SIGNATURES = {
     "fc_free_result": (None, [_FP]),
     "fc_set_shift_compat": (None, [_I]),
     "fc_set_generic_kernels": (None, [_I]),
+    "fc_set_host_io": (None, [_I]),
     "fc_set_l2_chunk_bytes": (None, [ctypes.c_longlong]),
     "fc_release_device": (_I, [_I]),
     "fc_version": (ctypes.c_char_p, []),

@@ -633,9 +633,50 @@ static void set_device(int dev) {
   cuda_check(cudaSetDevice(dev), "cudaSetDevice");
 }
 
+// Host I/O of the reference-compatible entry points.
+//   copy   (0): H2D of image and kernel into device buffers, D2H of the result;
+//   direct (1): the image x pass reads the caller's host buffer and the last
+//               pass writes the result into it, over the CPU-GPU link, with no
+//               staging copies -- for GPUs that access pageable host memory
+//               through the host page tables (GB300 with NVLink-C2C); used by
+//               the in-place entry only, whose buffer the caller has filled;
+//   auto   (2): the default; direct for page-locked (pinned or registered)
+//               host buffers, copy for pageable ones -- measured on GB300 at
+//               512x512x128: pinned direct 1.67 ms vs copy 1.78 ms, pageable
+//               direct 2.24 ms vs copy 1.88 ms per call.
+// direct never touches host memory through the GPU on a device that lacks
+// pageable-memory access: it falls back to copy there.
+// FC_HOST_IO=copy|direct|auto or fc_set_host_io() select it.
+static int g_host_io = -1;
+static int host_io_mode() {
+  if (g_host_io < 0) {
+    const char* e = std::getenv("FC_HOST_IO");
+    g_host_io = !e ? 2 : (std::strcmp(e, "direct") == 0 ? 1 : (std::strcmp(e, "copy") == 0 ? 0 : 2));
+  }
+  return g_host_io;
+}
+static bool device_reads_pageable(int dev) {
+  int a = 0, b = 0;
+  if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a == 1 && b == 1;
+}
+
+static bool host_buffer_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 // Host-pointer convolution used by the three reference-compatible entry points.
 static void host_conv(const float* im, float* out, int nx, int ny, int nz, const float* kernel, int kx, int ky,
-                      int kz, bool dense, int dev) {
+                      int kz, bool dense, int dev, bool allow_direct = false) {
   if (!im || !out || !kernel) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
   const Geom g = make_geom(nx, ny, nz, kx, ky, kz, dense);
   set_device(dev);
@@ -647,9 +688,15 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
   const size_t nimg = sizeof(float) * (size_t)g.N();
   const size_t nker = sizeof(float) * (dense ? (size_t)g.N() : (size_t)kx * ky * kz);
   grow(&c.ws, &c.ws_cap, wsb, "cudaMalloc(workspace)");
-  grow((void**)&c.d_img, &c.img_cap, nimg, "cudaMalloc(image)");
   grow((void**)&c.d_ker, &c.ker_cap, nker, "cudaMalloc(kernel)");
   cuda_check(cudaMemcpyAsync(c.d_ker, kernel, nker, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(kernel H2D)");
+  const int mode = host_io_mode();
+  if (allow_direct && mode != 0 && device_reads_pageable(dev) && (mode == 1 || host_buffer_pinned(im))) {
+    enqueue_conv(c, g, im, out, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
+    cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    return;
+  }
+  grow((void**)&c.d_img, &c.img_cap, nimg, "cudaMalloc(image)");
   cuda_check(cudaMemcpyAsync(c.d_img, im, nimg, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(image H2D)");
   enqueue_conv(c, g, c.d_img, c.d_img, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
   cuda_check(cudaMemcpyAsync(out, c.d_img, nimg, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync(result D2H)");
@@ -756,6 +803,7 @@ const char* fc_last_error(void) { return t_error.c_str(); }
 void fc_free_result(imageType* p) { delete[] p; }
 void fc_set_shift_compat(int on) { g_shift_compat = on ? 1 : 0; }
 void fc_set_generic_kernels(int on) { g_generic_only = on ? 1 : 0; }
+void fc_set_host_io(int mode) { g_host_io = (mode >= 0 && mode <= 2) ? mode : 2; }
 void fc_set_l2_chunk_bytes(long long bytes) { g_l2_chunk_bytes = bytes < 0 ? -1 : bytes; }
 const char* fc_version(void) { return "fc-gb300 0.1.0 (sm_103a)"; }
 int fc_launch_count(void) { return t_launches; }
@@ -807,7 +855,7 @@ void convolution3DfftCUDAInPlace(imageType* im, int* imDim, imageType* kernel, i
     int nx, ny, nz, kx, ky, kz;
     dims3(imDim, &nx, &ny, &nz);
     dims3(kernelDim, &kx, &ky, &kz);
-    host_conv(im, im, nx, ny, nz, kernel, kx, ky, kz, false, devCUDA);
+    host_conv(im, im, nx, ny, nz, kernel, kx, ky, kz, false, devCUDA, true);
   });
 }
 

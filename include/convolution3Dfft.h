@@ -106,6 +106,13 @@ FUNCTION_PREFIX void fc_set_shift_compat(int on);
    the generic shared-memory kernels elsewhere (default); 1 = generic kernels
    on every axis.  The environment variable FC_GENERIC=1 sets 1 at load time. */
 FUNCTION_PREFIX void fc_set_generic_kernels(int on);
+/* host I/O of convolution3DfftCUDAInPlace: 0 = copy the image to the device
+   and back; 1 = direct: the first pass reads the caller's buffer and the last
+   pass writes it over the CPU-GPU link, on GPUs that read pageable host memory
+   through the host page tables (e.g. GB300), copy elsewhere; 2 = auto
+   (default): direct for page-locked host buffers, copy for pageable ones.
+   FC_HOST_IO=copy|direct|auto sets it at load time. */
+FUNCTION_PREFIX void fc_set_host_io(int mode);
 /* L2 budget of one column chunk of the y / fused-z / y-inverse passes:
    0 = no chunking (default), -1 = half the device L2, else bytes.  The
    environment variable FC_L2_CHUNK_MB sets it at load time. */

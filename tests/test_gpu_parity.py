@@ -18,6 +18,16 @@ MAXABS_TOL = 1e-5
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["copy", "direct"])
+def host_io(request, fclib):
+    """convolution3DfftCUDAInPlace with staged copies, and with the passes
+    reading and writing the caller's host buffer directly (GB300 accesses
+    pageable host memory through the host page tables)."""
+    fclib.fc_set_host_io(0 if request.param == "copy" else 1)
+    yield request.param
+    fclib.fc_set_host_io(2)
+
+
 @pytest.fixture(params=["fast", "generic"])
 def kernels(request, fclib):
     """Run a test on the register-resident kernels (power-of-two axes) and on
@@ -44,7 +54,7 @@ def _gauss(k, s):
     return (g / g.sum()).astype(np.float32)
 
 
-def test_c1_plain_small_vs_fp64(cuda, orc, kernels):
+def test_c1_plain_small_vs_fp64(cuda, orc, kernels, host_io):
     # 64^3 uniform[0,1) (seed 1), 7^3 isotropic Gaussian sigma 1.5 normalised
     rng = np.random.Generator(np.random.PCG64(1))
     im = rng.random((64, 64, 64)).astype(np.float32)
@@ -85,7 +95,7 @@ def test_c1_vs_cufft_sequence(cuda, orc, kernels):
     ((16, 2048, 128), (3, 5, 3)),     # a 2048 column axis (generic kernels)
     ((256, 64, 32), (5, 3, 3)),       # short rows, long z
 ])
-def test_shapes_vs_fp64(cuda, orc, kernels, shape, kshape):
+def test_shapes_vs_fp64(cuda, orc, kernels, host_io, shape, kshape):
     rng = np.random.default_rng(sum(shape) + sum(kshape))
     im = rng.random(shape, dtype=np.float32)
     k = rng.random(kshape, dtype=np.float32)
@@ -98,7 +108,7 @@ def test_shapes_vs_fp64(cuda, orc, kernels, shape, kshape):
     _check(out, ref)
 
 
-def test_reference_kats(cuda, orc, kernels):
+def test_reference_kats(cuda, orc, kernels, host_io):
     """Every convolution known-answer case of the reference test suite, through
     convolution3DfftCUDAInPlace with the reference's padding protocol."""
     for case in orc.kat_cases(include_large=True):
