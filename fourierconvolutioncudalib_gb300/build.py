@@ -23,7 +23,7 @@ LIB_PATH = PKG / LIB_NAME
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", str(ROOT / "include")]
-SOURCES = ["fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu", "fc_noalloc.cu"]
+SOURCES = ["fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu", "fc_fast_zconv.cu", "fc_noalloc.cu"]
 
 
 def nvcc() -> str:
@@ -40,7 +40,8 @@ def _sources_mtime() -> float:
 
 def _compile(src: str, verbose: bool) -> Path:
     obj = BUILD / (Path(src).stem + ".o")
-    cmd = [nvcc(), *COMMON, *ARCH, "-c", str(CSRC / src), "-o", str(obj)]
+    extra = os.environ.get("FC_NVCC_EXTRA", "").split()  # e.g. -DFC_ZCONV_MIN_BLOCKS=3 for tuning builds
+    cmd = [nvcc(), *COMMON, *ARCH, *extra, "-c", str(CSRC / src), "-o", str(obj)]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     r = subprocess.run(cmd, capture_output=True, text=True)

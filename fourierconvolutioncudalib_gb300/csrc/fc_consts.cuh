@@ -133,6 +133,203 @@ template <> __device__ __forceinline__ float fc_dft_sin<13>(int j) {
   }
 }
 
+// cos(2*pi*j/R), sin(2*pi*j/R), j = 0..R-1, for the internal twiddles of the
+// composite butterflies R = A*B (Cooley-Tukey inside the registers).
+template <int R> __device__ __forceinline__ float fc_tw_cos(int j);
+template <int R> __device__ __forceinline__ float fc_tw_sin(int j);
+template <> __device__ __forceinline__ float fc_tw_cos<6>(int j) {
+  switch (j) {
+    case 0: return 1.0f;
+    case 1: return 0.5f;
+    case 2: return -0.5f;
+    case 3: return -1.0f;
+    case 4: return -0.5f;
+    case 5: return 0.5f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_sin<6>(int j) {
+  switch (j) {
+    case 0: return 0.0f;
+    case 1: return 0.8660253882408142f;
+    case 2: return 0.8660253882408142f;
+    case 3: return 1.2246468525851679e-16f;
+    case 4: return -0.8660253882408142f;
+    case 5: return -0.8660253882408142f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_cos<9>(int j) {
+  switch (j) {
+    case 0: return 1.0f;
+    case 1: return 0.7660444378852844f;
+    case 2: return 0.1736481785774231f;
+    case 3: return -0.5f;
+    case 4: return -0.9396926164627075f;
+    case 5: return -0.9396926164627075f;
+    case 6: return -0.5f;
+    case 7: return 0.1736481785774231f;
+    case 8: return 0.7660444378852844f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_sin<9>(int j) {
+  switch (j) {
+    case 0: return 0.0f;
+    case 1: return 0.6427876353263855f;
+    case 2: return 0.9848077297210693f;
+    case 3: return 0.8660253882408142f;
+    case 4: return 0.3420201539993286f;
+    case 5: return -0.3420201539993286f;
+    case 6: return -0.8660253882408142f;
+    case 7: return -0.9848077297210693f;
+    case 8: return -0.6427876353263855f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_cos<10>(int j) {
+  switch (j) {
+    case 0: return 1.0f;
+    case 1: return 0.80901700258255f;
+    case 2: return 0.30901700258255005f;
+    case 3: return -0.30901700258255005f;
+    case 4: return -0.80901700258255f;
+    case 5: return -1.0f;
+    case 6: return -0.80901700258255f;
+    case 7: return -0.30901700258255005f;
+    case 8: return 0.30901700258255005f;
+    case 9: return 0.80901700258255f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_sin<10>(int j) {
+  switch (j) {
+    case 0: return 0.0f;
+    case 1: return 0.5877852439880371f;
+    case 2: return 0.9510565400123596f;
+    case 3: return 0.9510565400123596f;
+    case 4: return 0.5877852439880371f;
+    case 5: return 1.2246468525851679e-16f;
+    case 6: return -0.5877852439880371f;
+    case 7: return -0.9510565400123596f;
+    case 8: return -0.9510565400123596f;
+    case 9: return -0.5877852439880371f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_cos<12>(int j) {
+  switch (j) {
+    case 0: return 1.0f;
+    case 1: return 0.8660253882408142f;
+    case 2: return 0.5f;
+    case 3: return 6.123234262925839e-17f;
+    case 4: return -0.5f;
+    case 5: return -0.8660253882408142f;
+    case 6: return -1.0f;
+    case 7: return -0.8660253882408142f;
+    case 8: return -0.5f;
+    case 9: return -1.8369701465288538e-16f;
+    case 10: return 0.5f;
+    case 11: return 0.8660253882408142f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_sin<12>(int j) {
+  switch (j) {
+    case 0: return 0.0f;
+    case 1: return 0.5f;
+    case 2: return 0.8660253882408142f;
+    case 3: return 1.0f;
+    case 4: return 0.8660253882408142f;
+    case 5: return 0.5f;
+    case 6: return 1.2246468525851679e-16f;
+    case 7: return -0.5f;
+    case 8: return -0.8660253882408142f;
+    case 9: return -1.0f;
+    case 10: return -0.8660253882408142f;
+    case 11: return -0.5f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_cos<14>(int j) {
+  switch (j) {
+    case 0: return 1.0f;
+    case 1: return 0.9009688496589661f;
+    case 2: return 0.6234897971153259f;
+    case 3: return 0.22252093255519867f;
+    case 4: return -0.22252093255519867f;
+    case 5: return -0.6234897971153259f;
+    case 6: return -0.9009688496589661f;
+    case 7: return -1.0f;
+    case 8: return -0.9009688496589661f;
+    case 9: return -0.6234897971153259f;
+    case 10: return -0.22252093255519867f;
+    case 11: return 0.22252093255519867f;
+    case 12: return 0.6234897971153259f;
+    case 13: return 0.9009688496589661f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_sin<14>(int j) {
+  switch (j) {
+    case 0: return 0.0f;
+    case 1: return 0.4338837265968323f;
+    case 2: return 0.7818315029144287f;
+    case 3: return 0.9749279022216797f;
+    case 4: return 0.9749279022216797f;
+    case 5: return 0.7818315029144287f;
+    case 6: return 0.4338837265968323f;
+    case 7: return 1.2246468525851679e-16f;
+    case 8: return -0.4338837265968323f;
+    case 9: return -0.7818315029144287f;
+    case 10: return -0.9749279022216797f;
+    case 11: return -0.9749279022216797f;
+    case 12: return -0.7818315029144287f;
+    case 13: return -0.4338837265968323f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_cos<15>(int j) {
+  switch (j) {
+    case 0: return 1.0f;
+    case 1: return 0.9135454297065735f;
+    case 2: return 0.6691306233406067f;
+    case 3: return 0.30901700258255005f;
+    case 4: return -0.10452846437692642f;
+    case 5: return -0.5f;
+    case 6: return -0.80901700258255f;
+    case 7: return -0.9781476259231567f;
+    case 8: return -0.9781476259231567f;
+    case 9: return -0.80901700258255f;
+    case 10: return -0.5f;
+    case 11: return -0.10452846437692642f;
+    case 12: return 0.30901700258255005f;
+    case 13: return 0.6691306233406067f;
+    case 14: return 0.9135454297065735f;
+    default: return 0.0f;
+  }
+}
+template <> __device__ __forceinline__ float fc_tw_sin<15>(int j) {
+  switch (j) {
+    case 0: return 0.0f;
+    case 1: return 0.4067366421222687f;
+    case 2: return 0.7431448101997375f;
+    case 3: return 0.9510565400123596f;
+    case 4: return 0.9945219159126282f;
+    case 5: return 0.8660253882408142f;
+    case 6: return 0.5877852439880371f;
+    case 7: return 0.2079116851091385f;
+    case 8: return -0.2079116851091385f;
+    case 9: return -0.5877852439880371f;
+    case 10: return -0.8660253882408142f;
+    case 11: return -0.9945219159126282f;
+    case 12: return -0.9510565400123596f;
+    case 13: return -0.7431448101997375f;
+    case 14: return -0.4067366421222687f;
+    default: return 0.0f;
+  }
+}
+
 // cos(2*pi*j/16), sin(2*pi*j/16) for the radix-16 internal twiddles.
 #define FC_C16_1 0.9238795042037964f
 #define FC_S16_1 0.3826834261417389f

@@ -1,49 +1,93 @@
-// Register-resident FFT building blocks for power-of-two lengths (sm_103a).
+// Register-resident FFT building blocks for lengths whose factors are all at
+// most 16 (sm_103a).
 //
-// A line of length N is held by T = N/E threads, E = min(16, N) complex values
-// per thread.  The stage chain is radix E, E, ..., then the remainder
-// (e.g. 512 = 16*16*2, 128 = 16*8).  At a stage of radix R the thread owns the
-// E/R butterflies j = t + b*T (b < E/R); register v[b*R + m] holds the
-// butterfly input x[j + m*N/R] before the stage and its output
-// y[(j - j%Ns)*R + j%Ns + m*Ns] after it (Stockham, natural order).
+// A length N has a compile-time radix chain R_0 .. R_{S-1} (largest radix
+// first, radices 2..16 including the composite 6, 9, 10, 12, 14, 15).  At a
+// stage of radix R each thread owns U = floor(16/R) butterflies
+// j = t + b*A (b < U, A = ceil((N/R)/U)); register v[b*R + m] holds the
+// butterfly input x[j + m*N/R] before the stage and the output
+// y[(j - j%Ns)*R + j%Ns + m*Ns] after it (Stockham, natural order).  A line
+// is held by T = max_s A_s threads with at most 16 values each.
 //
 // Consequences used by the pass kernels:
-//   * first stage inputs are x[t + m*T]: thread t loads them straight from
-//     global memory (consecutive t -> consecutive addresses);
-//   * last stage outputs are y[t + b*T + m*N/Rf]: stored straight to global
-//     memory, also coalesced;
-//   * between stages the values go once through shared memory (one write,
-//     one barrier, one read, one barrier), in a padded layout that is free of
-//     bank conflicts for both the row and the column tiles;
-//   * a forward transform's outputs are, up to a compile-time permutation of
-//     registers, exactly the inputs of the inverse transform's first stage, so
-//     a spectrum product between them never touches shared memory.
+//   * first stage inputs are x[j + m*N/R_0]: loaded straight from global
+//     memory (consecutive threads -> consecutive addresses);
+//   * last stage outputs are y[j + m*N/R_last]: stored straight to global;
+//   * between stages the values go once through shared memory (write,
+//     barrier, read, barrier) in a padded layout;
+//   * the inverse transform runs the reversed chain, so its first stage has
+//     the forward's last radix, thread split and positions: a spectrum product
+//     between a forward and an inverse transform happens in registers.
 #pragma once
 #include "fc_fft.cuh"
 
 namespace fc {
 namespace fast {
 
-template <int N>
-struct P2 {
-  static constexpr int E = N >= 16 ? 16 : N;
-  static constexpr int T = N / E;
-  // radix of the last stage
-  static constexpr int last_radix() {
-    int ns = 1;
-    while (true) {
-      const int rem = N / ns;
-      const int r = rem >= E ? E : rem;
-      if (ns * r >= N) return r;
-      ns *= r;
-    }
+constexpr int kVals = 16;  // values per thread
+
+__host__ __device__ constexpr int pick_radix(int rem) {
+  return rem % 16 == 0   ? 16
+         : rem % 15 == 0 ? 15
+         : rem % 14 == 0 ? 14
+         : rem % 13 == 0 ? 13
+         : rem % 12 == 0 ? 12
+         : rem % 11 == 0 ? 11
+         : rem % 10 == 0 ? 10
+         : rem % 9 == 0  ? 9
+         : rem % 8 == 0  ? 8
+         : rem % 7 == 0  ? 7
+         : rem % 6 == 0  ? 6
+         : rem % 5 == 0  ? 5
+         : rem % 4 == 0  ? 4
+         : rem % 3 == 0  ? 3
+         : rem % 2 == 0  ? 2
+                         : rem;
+}
+
+struct ChainC {
+  int len;
+  int r[12];
+};
+
+__host__ __device__ constexpr ChainC make_chain(int N) {
+  ChainC c{0, {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}};
+  int rem = N;
+  while (rem > 1 && c.len < 12) {
+    const int r = pick_radix(rem);
+    c.r[c.len++] = r;
+    rem /= r;
   }
-  static constexpr int RF = last_radix();
+  return c;
+}
+
+template <int N>
+struct Plan {
+  static constexpr ChainC C = make_chain(N);
+  static constexpr int S = C.len;
+  // stage i of the forward chain (REV = false) or of the reversed chain
+  __host__ __device__ static constexpr int radix(int i, bool rev) { return C.r[rev ? S - 1 - i : i]; }
+  __host__ __device__ static constexpr int U(int r) { return kVals / r; }
+  __host__ __device__ static constexpr int A(int r) { return ((N / r) + U(r) - 1) / U(r); }
+  __host__ __device__ static constexpr int max_a() {
+    int t = 1;
+    for (int i = 0; i < S; ++i) t = A(C.r[i]) > t ? A(C.r[i]) : t;
+    return t;
+  }
+  static constexpr int T = max_a();
+  __host__ __device__ static constexpr bool supported() {
+    if (N < 2) return false;
+    for (int i = 0; i < S; ++i)
+      if (C.r[i] > 16) return false;
+    int p = 1;
+    for (int i = 0; i < S; ++i) p *= C.r[i];
+    return p == N;
+  }
 };
 
 __device__ __forceinline__ int rpad(int i) { return i + (i >> 4); }
 
-// shared-memory index of logical position i of a row line (line base added by caller)
+// shared-memory view of one row line
 struct RowLay {
   float2* base;
   __device__ __forceinline__ float2& operator[](int i) const { return base[rpad(i)]; }
@@ -59,91 +103,94 @@ struct ColLay {
   }
 };
 
-template <int N, int E, int R, int NS, bool INV>
-__device__ __forceinline__ void stage(float2 (&v)[E], const int t, const float2* __restrict__ W) {
-  constexpr int T = N / E;
+template <int N, int R, int NS, bool INV>
+__device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const float2* __restrict__ W) {
+  constexpr int U = kVals / R;
+  constexpr int A = Plan<N>::A(R);
+  constexpr int NB = N / R;
   constexpr int TWS = N / (NS * R);
+  // butterflies a thread does not own compute on stale registers and are never stored;
+  // their twiddle index stays below N
 #pragma unroll
-  for (int b = 0; b < E / R; ++b) {
+  for (int b = 0; b < U; ++b) {
     if (NS > 1) {
-      const int j = t + b * T;
-      const int k = j & (NS - 1);
+      const int k = (t + b * A) % NS;
 #pragma unroll
       for (int r = 1; r < R; ++r) v[b * R + r] = c_tw<INV>(v[b * R + r], __ldg(W + k * r * TWS));
     }
     Dft<R, INV>::run(&v[b * R]);
   }
+  (void)NB;
 }
 
-template <int N, int E, int R, int NS, int R2, class L>
-__device__ __forceinline__ void exchange(float2 (&v)[E], const L& sm, const int t) {
-  constexpr int T = N / E;
+template <int N, int R, int NS, int R2, class L>
+__device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const int t) {
+  constexpr int U = kVals / R, A = Plan<N>::A(R), NB = N / R;
+  constexpr int U2 = kVals / R2, A2 = Plan<N>::A(R2), NB2 = N / R2;
 #pragma unroll
-  for (int b = 0; b < E / R; ++b) {
-    const int j = t + b * T;
-    const int k = j & (NS - 1);
-    const int base = (j - k) * R + k;
+  for (int b = 0; b < U; ++b) {
+    const int j = t + b * A;
+    if (j < NB && t < A) {
+      const int k = j % NS;
+      const int base = (j - k) * R + k;
 #pragma unroll
-    for (int m = 0; m < R; ++m) sm[base + m * NS] = v[b * R + m];
+      for (int m = 0; m < R; ++m) sm[base + m * NS] = v[b * R + m];
+    }
   }
   __syncthreads();
 #pragma unroll
-  for (int b = 0; b < E / R2; ++b) {
-    const int j = t + b * T;
+  for (int b = 0; b < U2; ++b) {
+    const int j = t + b * A2;
+    if (j < NB2 && t < A2) {
 #pragma unroll
-    for (int m = 0; m < R2; ++m) v[b * R2 + m] = sm[j + m * (N / R2)];
+      for (int m = 0; m < R2; ++m) v[b * R2 + m] = sm[j + m * NB2];
+    }
   }
   __syncthreads();
 }
 
-// Run the stages from sub-transform size NS to the end.
-template <int N, int NS, bool INV>
+// stages I .. S-1 of the forward chain (INV = false) or of the reversed chain (INV = true)
+template <int N, int I, int NS, bool INV>
 struct Chain {
-  static constexpr int E = P2<N>::E;
   template <class L>
-  static __device__ __forceinline__ void run(float2 (&v)[E], const L& sm, const int t,
+  static __device__ __forceinline__ void run(float2 (&v)[kVals], const L& sm, const int t,
                                              const float2* __restrict__ W) {
-    constexpr int REM = N / NS;
-    constexpr int R = REM >= E ? E : REM;
-    stage<N, E, R, NS, INV>(v, t, W);
-    if constexpr (NS * R < N) {
-      constexpr int NS2 = NS * R;
-      constexpr int REM2 = N / NS2;
-      constexpr int R2 = REM2 >= E ? E : REM2;
-      exchange<N, E, R, NS, R2>(v, sm, t);
-      Chain<N, NS2, INV>::run(v, sm, t, W);
+    constexpr int R = Plan<N>::radix(I, INV);
+    stage<N, R, NS, INV>(v, t, W);
+    if constexpr (I + 1 < Plan<N>::S) {
+      constexpr int R2 = Plan<N>::radix(I + 1, INV);
+      exchange<N, R, NS, R2>(v, sm, t);
+      Chain<N, I + 1, NS * R, INV>::run(v, sm, t, W);
     }
   }
 };
 
-// full transform: v[m] = x[t + m*T] in, v[b*RF + m] = X[t + b*T + m*N/RF] out
+// full transform; inputs per first_pos, outputs per last_pos
 template <int N, bool INV, class L>
-__device__ __forceinline__ void fft(float2 (&v)[P2<N>::E], const L& sm, const int t, const float2* __restrict__ W) {
-  Chain<N, 1, INV>::run(v, sm, t, W);
+__device__ __forceinline__ void fft(float2 (&v)[kVals], const L& sm, const int t, const float2* __restrict__ W) {
+  Chain<N, 0, 1, INV>::run(v, sm, t, W);
 }
 
-// logical position of output register index q (= b*RF + m)
-template <int N>
-__device__ __forceinline__ int out_pos(const int t, const int q) {
-  constexpr int RF = P2<N>::RF;
-  return t + (q / RF) * P2<N>::T + (q % RF) * (N / RF);
+// radix of the first / last stage of the forward (INV=false) or inverse chain
+template <int N, bool INV>
+__host__ __device__ constexpr int first_radix() {
+  return Plan<N>::radix(0, INV);
+}
+template <int N, bool INV>
+__host__ __device__ constexpr int last_radix() {
+  return Plan<N>::radix(Plan<N>::S - 1, INV);
 }
 
-// reorder forward outputs into the inverse's first-stage input order:
-// out register b*RF + m holds position t + T*(b + m*E/RF), the inverse's input m' = b + m*E/RF
-template <int N>
-__device__ __forceinline__ void out_to_in(float2 (&v)[P2<N>::E]) {
-  constexpr int E = P2<N>::E;
-  constexpr int RF = P2<N>::RF;
-  if constexpr (RF != E) {
-    float2 w[E];
-#pragma unroll
-    for (int b = 0; b < E / RF; ++b)
-#pragma unroll
-      for (int m = 0; m < RF; ++m) w[b + m * (E / RF)] = v[b * RF + m];
-#pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = w[i];
-  }
+// Register q = b*R + m of a stage of radix R (first stage: input position;
+// last stage: output position) is position j + m*N/R with j = t + b*A(R);
+// returns -1 when the butterfly does not exist for this thread.
+template <int N, int R>
+__device__ __forceinline__ int stage_pos(const int t, const int q) {
+  constexpr int A = Plan<N>::A(R);
+  const int b = q / R, m = q % R;
+  const int j = t + b * A;
+  if (q >= (kVals / R) * R || t >= A || j >= N / R) return -1;
+  return j + m * (N / R);
 }
 
 }  // namespace fast

@@ -1,0 +1,186 @@
+// Register-resident column-pass kernel templates (lengths in FC_COL_SIZES):
+// the y passes, the fused z pass (forward image and kernel columns, the
+// reference's modulate-and-normalise, inverse) and the kernel-gradient z
+// pass.  Instantiated by fc_fast_cols.cu and fc_fast_zconv.cu.
+//
+// A CTA owns B adjacent columns (kx) of one plane; thread (c, t) holds up to
+// 16 values of column c (positions per the stage split of fc_fast.cuh).
+// Global loads and stores are B*8 contiguous bytes per row; shared memory is
+// an N x B tile in a padded layout used only for the exchanges between radix
+// stages.
+#pragma once
+#ifndef FC_ZCONV_MIN_BLOCKS
+#define FC_ZCONV_MIN_BLOCKS 2
+#endif
+#include "fc_fast.cuh"
+#include "fc_fast_sizes.h"
+#include "fc_internal.h"
+#include "fc_sources.cuh"
+
+namespace fc {
+namespace fast {
+
+template <int N>
+struct ColGeom {
+  static constexpr int T = Plan<N>::T;
+  // columns per tile: a power of two with N*B ~ 4096 values, between 4 and 32
+  static constexpr int B0 = 4096 / N;
+  static constexpr int B = B0 >= 32 ? 32 : B0 >= 16 ? 16 : B0 >= 8 ? 8 : 4;
+  static constexpr int THREADS = B * T;
+  static constexpr int SMEM = N * B + (N * B) / 16;  // float2 elements
+};
+
+template <int N, bool INV, class Src>
+__global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* dst, long long ps,
+                                                              long long es, int ncols, const float2* __restrict__ W) {
+  using G = ColGeom<N>;
+  constexpr int B = G::B;
+  constexpr int R0 = first_radix<N, INV>(), RF = last_radix<N, INV>();
+  __shared__ float2 sm[G::SMEM];
+  const int c = threadIdx.x % B;
+  const int t = threadIdx.x / B;
+  const int col = blockIdx.x * B + c;
+  const int plane = blockIdx.y;
+  const bool ok = col < ncols;
+  float2 v[kVals];
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) {
+    const int j = stage_pos<N, R0>(t, q);
+    v[q] = (ok && j >= 0) ? src.load(plane, j, col) : make_float2(0.f, 0.f);
+  }
+  fft<N, INV>(v, ColLay<B>{sm, c}, t, W);
+  if (ok) {
+    float2* d = dst + (long long)plane * ps + col;
+#pragma unroll
+    for (int q = 0; q < kVals; ++q) {
+      const int j = stage_pos<N, RF>(t, q);
+      if (j >= 0) d[(long long)j * es] = v[q];
+    }
+  }
+}
+
+// Fused z pass.  Kernel plane p of KXY holds z = (p - hz) mod nz.  The
+// kernel column is transformed first and parked in a per-thread private
+// shared-memory stash (stash[q*THREADS + tid], no barrier needed), so only
+// one column's values are live in registers during the image transform.
+template <int N>
+struct ZGeom {
+  static constexpr int SMEM_BYTES = (ColGeom<N>::SMEM + ColGeom<N>::THREADS * kVals) * (int)sizeof(float2);
+  // resident CTAs requested from the register allocator (256 threads: 2 -> <= 128 registers)
+  static constexpr int MIN_BLOCKS = ColGeom<N>::THREADS <= 256 ? FC_ZCONV_MIN_BLOCKS : 1;
+};
+
+template <int N, bool CONJ>
+__global__ void __launch_bounds__(ColGeom<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zconv(float2* __restrict__ S, const float2* __restrict__ KXY,
+                                                               long long pitch, int ny, int ncols, int kplanes, int hz,
+                                                               float scale, const float2* __restrict__ W) {
+  using G = ColGeom<N>;
+  constexpr int B = G::B;
+  constexpr int R0 = first_radix<N, false>(), RF = last_radix<N, true>();
+  extern __shared__ float2 zsm[];
+  float2* sm = zsm;
+  float2* stash = zsm + G::SMEM;
+  const int tid = threadIdx.x;
+  const int c = tid % B;
+  const int t = tid / B;
+  const int col = blockIdx.x * B + c;
+  const int ky = blockIdx.y;
+  const bool ok = col < ncols;
+  const long long zs = (long long)ny * pitch;
+  float2* base = S + (long long)ky * pitch + col;
+  const ColLay<B> lay{sm, c};
+  float2 v[kVals];
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) {
+    const int z = stage_pos<N, R0>(t, q);
+    int p = z + hz;
+    if (p >= N) p -= N;
+    v[q] = (ok && z >= 0 && p < kplanes) ? KXY[((long long)p * ny + ky) * pitch + col] : make_float2(0.f, 0.f);
+  }
+  fft<N, false>(v, lay, t, W);
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) stash[q * G::THREADS + tid] = v[q];
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) {
+    const int z = stage_pos<N, R0>(t, q);
+    v[q] = (ok && z >= 0) ? base[z * zs] : make_float2(0.f, 0.f);
+  }
+  fft<N, false>(v, lay, t, W);
+  // the forward outputs sit where the inverse's first stage reads them
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) {
+    float2 a = stash[q * G::THREADS + tid];  // kernel spectrum (d_Src of modulateAndNormalize_kernel)
+    const float2 b = v[q];                   // image spectrum  (d_Dst)
+    if (CONJ) a.y = -a.y;
+    v[q] = make_float2(scale * (a.x * b.x - a.y * b.y), scale * (a.y * b.x + a.x * b.y));
+  }
+  fft<N, true>(v, lay, t, W);
+  if (ok) {
+#pragma unroll
+    for (int q = 0; q < kVals; ++q) {
+      const int z = stage_pos<N, RF>(t, q);
+      if (z >= 0) base[(long long)z * zs] = v[q];
+    }
+  }
+}
+
+// Kernel-gradient z pass: conj(X) * G * scale, inverse, keep kernel planes
+// p < kz where z = (p - hz) mod nz, written to out plane p.
+template <int N>
+__global__ void __launch_bounds__(ColGeom<N>::THREADS) k_zcorr(const float2* __restrict__ X,
+                                                               const float2* __restrict__ Gs, float2* __restrict__ out,
+                                                               long long pitch, int ny, int ncols, int kz, int hz,
+                                                               float scale, const float2* __restrict__ W) {
+  using G = ColGeom<N>;
+  constexpr int B = G::B;
+  constexpr int R0 = first_radix<N, false>(), RF = last_radix<N, true>();
+  extern __shared__ float2 zsm[];
+  float2* sm = zsm;
+  float2* stash = zsm + G::SMEM;
+  const int tid = threadIdx.x;
+  const int c = tid % B;
+  const int t = tid / B;
+  const int col = blockIdx.x * B + c;
+  const int ky = blockIdx.y;
+  const bool ok = col < ncols;
+  const long long zs = (long long)ny * pitch;
+  const long long off = (long long)ky * pitch + col;
+  float2 v[kVals];
+  const ColLay<B> lay{sm, c};
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) {
+    const int z = stage_pos<N, R0>(t, q);
+    v[q] = (ok && z >= 0) ? X[(long long)z * zs + off] : make_float2(0.f, 0.f);
+  }
+  fft<N, false>(v, lay, t, W);
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) stash[q * G::THREADS + tid] = v[q];
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) {
+    const int z = stage_pos<N, R0>(t, q);
+    v[q] = (ok && z >= 0) ? Gs[(long long)z * zs + off] : make_float2(0.f, 0.f);
+  }
+  fft<N, false>(v, lay, t, W);
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) {
+    const float2 x = stash[q * G::THREADS + tid];
+    const float2 a = make_float2(x.x, -x.y);
+    const float2 b = v[q];
+    v[q] = make_float2(scale * (a.x * b.x - a.y * b.y), scale * (a.y * b.x + a.x * b.y));
+  }
+  fft<N, true>(v, lay, t, W);
+  if (ok) {
+#pragma unroll
+    for (int q = 0; q < kVals; ++q) {
+      const int z = stage_pos<N, RF>(t, q);
+      if (z < 0) continue;
+      int p = z + hz;
+      if (p >= N) p -= N;
+      if (p < kz) out[((long long)p * ny + ky) * pitch + col] = v[q];
+    }
+  }
+}
+
+
+}  // namespace fast
+}  // namespace fc

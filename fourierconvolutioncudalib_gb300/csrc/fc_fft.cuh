@@ -164,11 +164,51 @@ template <int P, bool INV> struct DftOdd {
     v[0] = X0;
   }
 };
+// composite R = A*B: X[k1 + A k2] = sum_n2 wB^(n2 k2) wR^(n2 k1) sum_n1 x[B n1 + n2] wA^(n1 k1)
+template <int A, int B, bool INV> struct DftCT {
+  static constexpr int R = A * B;
+  static __device__ __forceinline__ void run(float2* v) {
+    float2 y[B][A];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+      float2 t[A];
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) t[n1] = v[B * n1 + n2];
+      Dft<A, INV>::run(t);
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) {
+        const int e = (n2 * k1) % R;
+        if (e == 0) {
+          y[n2][k1] = t[k1];
+        } else {
+          const float2 w = make_float2(fc_tw_cos<R>(e), (INV ? 1.0f : -1.0f) * fc_tw_sin<R>(e));
+          y[n2][k1] = c_mul(t[k1], w);
+        }
+      }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+      float2 t[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) t[n2] = y[n2][k1];
+      Dft<B, INV>::run(t);
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) v[k1 + A * k2] = t[k2];
+    }
+  }
+};
+
 template <bool INV> struct Dft<3, INV> : DftOdd<3, INV> {};
 template <bool INV> struct Dft<5, INV> : DftOdd<5, INV> {};
 template <bool INV> struct Dft<7, INV> : DftOdd<7, INV> {};
 template <bool INV> struct Dft<11, INV> : DftOdd<11, INV> {};
 template <bool INV> struct Dft<13, INV> : DftOdd<13, INV> {};
+template <bool INV> struct Dft<6, INV> : DftCT<2, 3, INV> {};
+template <bool INV> struct Dft<9, INV> : DftCT<3, 3, INV> {};
+template <bool INV> struct Dft<10, INV> : DftCT<2, 5, INV> {};
+template <bool INV> struct Dft<12, INV> : DftCT<4, 3, INV> {};
+template <bool INV> struct Dft<14, INV> : DftCT<2, 7, INV> {};
+template <bool INV> struct Dft<15, INV> : DftCT<3, 5, INV> {};
 
 // ---------------------------------------------------------------- stages
 // One Stockham stage of radix R over all lines of a tile.

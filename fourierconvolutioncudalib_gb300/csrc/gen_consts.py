@@ -1,8 +1,8 @@
 """Generate fc_consts.cuh: the DFT constants of the in-register butterflies.
 
 The values are cos(2*pi*j/P) and sin(2*pi*j/P) for the odd prime radices
-P = 3, 5, 7, 11, 13 and the internal twiddles of the radix-16 butterfly
-(exp(-2*pi*i*j/16)).  They are evaluated in double precision with Python's
+P = 3, 5, 7, 11, 13, the internal twiddles of the composite radices
+6, 9, 10, 12, 14, 15 and of the radix-16 butterfly (exp(-2*pi*i*j/16)).  They are evaluated in double precision with Python's
 math module and rounded once to float32 (repr of the float32 value, so the
 literal is exact).  Run:  python gen_consts.py > fc_consts.cuh
 """
@@ -40,6 +40,14 @@ def main() -> None:
     for p in (3, 5, 7, 11, 13):
         out.append(emit_table("fc_dft_cos", p, math.cos))
         out.append(emit_table("fc_dft_sin", p, math.sin))
+    out.append("")
+    out.append("// cos(2*pi*j/R), sin(2*pi*j/R), j = 0..R-1, for the internal twiddles of the")
+    out.append("// composite butterflies R = A*B (Cooley-Tukey inside the registers).")
+    out.append("template <int R> __device__ __forceinline__ float fc_tw_cos(int j);")
+    out.append("template <int R> __device__ __forceinline__ float fc_tw_sin(int j);")
+    for r in (6, 9, 10, 12, 14, 15):
+        out.append(emit_table("fc_tw_cos", r, math.cos))
+        out.append(emit_table("fc_tw_sin", r, math.sin))
     out.append("")
     out.append("// cos(2*pi*j/16), sin(2*pi*j/16) for the radix-16 internal twiddles.")
     out.append("#define FC_C16_1 " + f32(math.cos(2 * math.pi / 16)))

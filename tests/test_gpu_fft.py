@@ -19,7 +19,7 @@ SHAPES = [  # (z, y, x)
     (7, 49, 343),   # power_of_7 (:353-384)
     (128, 128, 128),  # cube_128_shape (:386-416)
     (7, 14, 343),   # out-of-place variant shape
-    (128, 512, 512), (96, 448, 384), (1, 1, 64), (2, 3, 4), (1, 1, 1), (8, 16, 4096), (4, 1024, 32),
+    (128, 512, 512), (96, 448, 384), (1, 1, 64), (2, 3, 4), (1, 1, 1), (8, 16, 4096), (4, 1024, 32), (160, 288, 320), (200, 352, 400), (12, 960, 768),
 ]
 
 

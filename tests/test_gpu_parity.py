@@ -94,6 +94,10 @@ def test_c1_vs_cufft_sequence(cuda, orc, kernels):
     ((64, 256, 1024), (9, 9, 9)),     # 1024 rows
     ((16, 2048, 128), (3, 5, 3)),     # a 2048 column axis (generic kernels)
     ((256, 64, 32), (5, 3, 3)),       # short rows, long z
+    ((96, 448, 384), (63, 31, 31)),   # the non-power-of-two microscope configuration (radices 16, 14, 12, 6, 2)
+    ((160, 288, 320), (21, 25, 23)),  # batch-view lengths: radices 10 and 9
+    ((64, 352, 400), (9, 11, 13)),    # radices 11 and 5
+    ((200, 96, 224), (7, 5, 9)),      # radix 10 chain along z, 14 along x
 ])
 def test_shapes_vs_fp64(cuda, orc, kernels, host_io, shape, kshape):
     rng = np.random.default_rng(sum(shape) + sum(kshape))
