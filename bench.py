@@ -328,6 +328,14 @@ def run_ours(args, cfg, world, rank, local):
         except Exception as e:  # the cuFFT harness is optional for the line
             ref_cufft = {"error": str(e)[:200]}
 
+    # ---- the other forms (adjoint, batched) against the plain path on the same GPU
+    forms = None
+    if rank == 0 and not args.no_forms:
+        try:
+            forms = time_forms(dev, fcd, torch)
+        except Exception as e:  # reported, not fatal for the headline line
+            forms = {"error": str(e)[:300]}
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -343,6 +351,7 @@ def run_ours(args, cfg, world, rank, local):
                                                          "step events)", "parallelism": f"replicas x{world}"},
             "wall_s_timed_region": t1 - t0,
             "e2e": e2e, "roofline": roofline, "passes": table, "cpu_baseline": cpu, "ref_cufft": ref_cufft,
+            "forms": forms,
             "gpu_launches": launches, "clocks": clocks.summary(t0, t1),
         }
         print(json.dumps(line), flush=True)
@@ -393,6 +402,99 @@ def time_ref_cufft(im_np, k_np, dev, args, our_value):
             "what": "cuFFT 3D R2C(image), R2C(padded kernel), modulate x 1/N, C2R; plans pre-built"}
 
 
+def _events_ms(torch, fn, reps, flush):
+    st = torch.cuda.current_stream()
+    ts = []
+    for i in range(reps + 2):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        if i >= 2:
+            ts.append(a.elapsed_time(b))
+    return statistics.mean(ts)
+
+
+def _rel64(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def _fp64_conv(im, k):
+    """Circular convolution in double precision (numpy), kernel centre at k//2."""
+    pk = np.zeros(im.shape, np.float64)
+    kz, ky, kx = k.shape
+    nz, ny, nx = im.shape
+    pk[np.ix_((np.arange(kz) - kz // 2) % nz, (np.arange(ky) - ky // 2) % ny, (np.arange(kx) - kx // 2) % nx)] = k
+    ax = (0, 1, 2)
+    return np.fft.irfftn(np.fft.rfftn(im.astype(np.float64)) * np.fft.rfftn(pk), s=im.shape, axes=ax), pk
+
+
+def time_forms(dev, fcd, torch):
+    """Adjoint form on the differentiation configuration (256^3, 21^3) and the
+    batched form on the multi-view configuration (6 uneven views), each
+    against the plain path on the same GPU, with its error against FP64."""
+    from fourierconvolutioncudalib_gb300 import workloads as W
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    out = {}
+    # adjoint: both gradients of 0.5*||conv(x,k) - y||^2 for a given residual
+    d = W.c3()
+    x, k = d["image"], d["kernel"]
+    rng = np.random.default_rng(44)
+    g = rng.standard_normal(x.shape).astype(np.float32)
+    xt, kt, gt = (torch.from_numpy(a).to(dev) for a in (x, k, g))
+    ms_adj = _events_ms(torch, lambda: fcd.conv3d_adjoint(xt, kt, gt, k.shape), 10, flush)
+    ms_fwd = _events_ms(torch, lambda: fcd.conv3d(xt, kt), 10, flush)
+    gi, gk = fcd.conv3d_adjoint(xt, kt, gt, k.shape)
+    torch.cuda.synchronize()
+    _, pk = _fp64_conv(x, k)
+    G = np.fft.rfftn(g.astype(np.float64))
+    ax = (0, 1, 2)
+    ex = np.fft.irfftn(G * np.conj(np.fft.rfftn(pk)), s=x.shape, axes=ax)
+    gP = np.fft.irfftn(np.conj(np.fft.rfftn(x.astype(np.float64))) * G, s=x.shape, axes=ax)
+    kz, ky, kx = k.shape
+    nz, ny, nx = x.shape
+    ek = gP[np.ix_((np.arange(kz) - kz // 2) % nz, (np.arange(ky) - ky // 2) % ny, (np.arange(kx) - kx // 2) % nx)]
+    out["adjoint"] = {"workload": "adjoint_256x256x256_psf21x21x21", "value": x.size / (ms_adj / 1e3) / 1e9,
+                      "unit": "Gvoxel/s", "ms": ms_adj, "plain_forward_ms": ms_fwd,
+                      "vs_plain": ms_fwd / ms_adj,
+                      "fp64_rel_l2_grad_image": _rel64(gi.cpu().numpy(), ex),
+                      "fp64_rel_l2_grad_kernel": _rel64(gk.cpu().numpy(), ek)}
+    # batched: six views, one call, against six sequential plain calls
+    views = W.c4()
+    imgs = [torch.from_numpy(v["image"]).to(dev) for v in views]
+    kers = [torch.from_numpy(v["kernel"]).to(dev) for v in views]
+    outs = [torch.empty_like(i) for i in imgs]
+    dims = []
+    for i, kk in zip(imgs, kers):
+        dims += [i.shape[2], i.shape[1], i.shape[0], kk.shape[2], kk.shape[1], kk.shape[0]]
+    need = fcd.lib().fc_conv3d_batched_workspace_bytes(len(imgs), fcd._iarr(dims), 0)
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    ws1 = torch.empty(max(fcd.workspace_bytes(i.shape, kk.shape) for i, kk in zip(imgs, kers)), dtype=torch.uint8,
+                      device=dev)
+    nvox = sum(i.numel() for i in imgs)
+    ms_b = _events_ms(torch, lambda: fcd.conv3d_batched(imgs, kers, outs=outs, workspace=ws), 10, flush)
+
+    def seq():
+        for i, kk, o in zip(imgs, kers, outs):
+            fcd.conv3d(i, kk, out=o, workspace=ws1)
+
+    ms_s = _events_ms(torch, seq, 10, flush)
+    fcd.conv3d_batched(imgs, kers, outs=outs, workspace=ws)
+    torch.cuda.synchronize()
+    errs = [_rel64(o.cpu().numpy(), _fp64_conv(v["image"], v["kernel"])[0]) for o, v in zip(outs, views)]
+    out["batched"] = {"workload": "batched_6_views_87M_voxels", "value": nvox / (ms_b / 1e3) / 1e9,
+                      "unit": "Gvoxel/s", "ms": ms_b, "sequential_plain_ms": ms_s, "vs_sequential_plain": ms_s / ms_b,
+                      "fp64_rel_l2_max_over_views": max(errs),
+                      "how": "one persistent launch per pass over a device work-list, CUDA graph replay"}
+    out["tensor_core"] = {"unavailable": "tensor-core DFT stages not built yet"}
+    return out
+
+
 def time_cpu_baseline(im_np, k_np):
     from oracle import oracle as orc
 
@@ -422,6 +524,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ref-cufft", action="store_true")
+    ap.add_argument("--no-forms", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

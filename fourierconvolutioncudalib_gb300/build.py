@@ -23,7 +23,9 @@ LIB_PATH = PKG / LIB_NAME
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", str(ROOT / "include")]
-SOURCES = ["fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu", "fc_fast_zconv.cu", "fc_noalloc.cu"]
+SOURCES = ["fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu", "fc_fast_zconv.cu", "fc_fast_zadj.cu",
+           "fc_batched_rows_fwd.cu", "fc_batched_rows_inv.cu", "fc_batched_cols_fwd.cu", "fc_batched_cols_inv.cu",
+           "fc_batched_zconv.cu", "fc_noalloc.cu"]
 
 
 def nvcc() -> str:
@@ -55,8 +57,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= _sources_mtime():
         return LIB_PATH
     BUILD.mkdir(exist_ok=True)
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    workers = min(len(SOURCES), os.cpu_count() or 4)
+    # longest translation units first
+    order = sorted(SOURCES, key=lambda f: 0 if f.startswith(("fc_batched", "fc_fast_z")) else 1)
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), order))
     tmp = BUILD / (LIB_NAME + ".tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs), "-lpthread", "-ldl", "-lrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)

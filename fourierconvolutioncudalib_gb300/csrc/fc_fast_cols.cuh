@@ -23,25 +23,26 @@ namespace fast {
 template <int N>
 struct ColGeom {
   static constexpr int T = Plan<N>::T;
-  // columns per tile: a power of two with N*B ~ 4096 values, between 4 and 32
-  static constexpr int B0 = 4096 / N;
+  // columns per tile: the largest power of two <= 32 with N*B <= 4096 values
+  // and B*T <= 256 threads (4 at least)
+  static constexpr int B0a = 4096 / N, B0b = 256 / T;
+  static constexpr int B0 = B0a < B0b ? B0a : B0b;
   static constexpr int B = B0 >= 32 ? 32 : B0 >= 16 ? 16 : B0 >= 8 ? 8 : 4;
   static constexpr int THREADS = B * T;
-  static constexpr int SMEM = N * B + (N * B) / 16;  // float2 elements
+  static constexpr int SMEM = N * B + (N * B) / 16;  // float2 elements of the exchange tile
 };
 
+// y pass body: tile (bx, plane) = columns [bx*B, bx*B + B) of one plane.
 template <int N, bool INV, class Src>
-__global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* dst, long long ps,
-                                                              long long es, int ncols, const float2* __restrict__ W) {
+__device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long ps, long long es, int ncols,
+                                          const float2* __restrict__ W, int bx, int plane, int tid, float2* sm) {
   using G = ColGeom<N>;
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, INV>(), RF = last_radix<N, INV>();
-  __shared__ float2 sm[G::SMEM];
-  const int c = threadIdx.x % B;
-  const int t = threadIdx.x / B;
-  const int col = blockIdx.x * B + c;
-  const int plane = blockIdx.y;
-  const bool ok = col < ncols;
+  const int c = tid % B;
+  const int t = tid / B;  // >= T for threads beyond the tile: they own no butterfly
+  const int col = bx * B + c;
+  const bool ok = col < ncols && t < G::T;
   float2 v[kVals];
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
@@ -59,6 +60,13 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* d
   }
 }
 
+template <int N, bool INV, class Src>
+__global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* dst, long long ps, long long es,
+                                                              int ncols, const float2* __restrict__ W) {
+  __shared__ float2 sm[ColGeom<N>::SMEM];
+  body_cols<N, INV>(src, dst, ps, es, ncols, W, (int)blockIdx.x, (int)blockIdx.y, (int)threadIdx.x, sm);
+}
+
 // Fused z pass.  Kernel plane p of KXY holds z = (p - hz) mod nz.  The
 // kernel column is transformed first and parked in a per-thread private
 // shared-memory stash (stash[q*THREADS + tid], no barrier needed), so only
@@ -70,22 +78,19 @@ struct ZGeom {
   static constexpr int MIN_BLOCKS = ColGeom<N>::THREADS <= 256 ? FC_ZCONV_MIN_BLOCKS : 1;
 };
 
+// fused z pass body: tile (bx, ky); stash holds nstash >= THREADS slots per value index
 template <int N, bool CONJ>
-__global__ void __launch_bounds__(ColGeom<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zconv(float2* __restrict__ S, const float2* __restrict__ KXY,
-                                                               long long pitch, int ny, int ncols, int kplanes, int hz,
-                                                               float scale, const float2* __restrict__ W) {
+__device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch,
+                                           int ny, int ncols, int kplanes, int hz, float scale,
+                                           const float2* __restrict__ W, int bx, int ky, int tid, float2* sm,
+                                           float2* stash, int nstash) {
   using G = ColGeom<N>;
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, false>(), RF = last_radix<N, true>();
-  extern __shared__ float2 zsm[];
-  float2* sm = zsm;
-  float2* stash = zsm + G::SMEM;
-  const int tid = threadIdx.x;
   const int c = tid % B;
   const int t = tid / B;
-  const int col = blockIdx.x * B + c;
-  const int ky = blockIdx.y;
-  const bool ok = col < ncols;
+  const int col = bx * B + c;
+  const bool ok = col < ncols && t < G::T;
   const long long zs = (long long)ny * pitch;
   float2* base = S + (long long)ky * pitch + col;
   const ColLay<B> lay{sm, c};
@@ -99,7 +104,7 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_z
   }
   fft<N, false>(v, lay, t, W);
 #pragma unroll
-  for (int q = 0; q < kVals; ++q) stash[q * G::THREADS + tid] = v[q];
+  for (int q = 0; q < kVals; ++q) stash[q * nstash + tid] = v[q];
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int z = stage_pos<N, R0>(t, q);
@@ -109,8 +114,8 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_z
   // the forward outputs sit where the inverse's first stage reads them
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
-    float2 a = stash[q * G::THREADS + tid];  // kernel spectrum (d_Src of modulateAndNormalize_kernel)
-    const float2 b = v[q];                   // image spectrum  (d_Dst)
+    float2 a = stash[q * nstash + tid];  // kernel spectrum (d_Src of modulateAndNormalize_kernel)
+    const float2 b = v[q];               // image spectrum  (d_Dst)
     if (CONJ) a.y = -a.y;
     v[q] = make_float2(scale * (a.x * b.x - a.y * b.y), scale * (a.y * b.x + a.x * b.y));
   }
@@ -122,6 +127,15 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_z
       if (z >= 0) base[(long long)z * zs] = v[q];
     }
   }
+}
+
+template <int N, bool CONJ>
+__global__ void __launch_bounds__(ColGeom<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zconv(
+    float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+    float scale, const float2* __restrict__ W) {
+  extern __shared__ float2 zsm[];
+  body_zconv<N, CONJ>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, W, (int)blockIdx.x, (int)blockIdx.y,
+                      (int)threadIdx.x, zsm, zsm + ColGeom<N>::SMEM, ColGeom<N>::THREADS);
 }
 
 // Kernel-gradient z pass: conj(X) * G * scale, inverse, keep kernel planes
@@ -142,7 +156,7 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_zcorr(const float2* __r
   const int t = tid / B;
   const int col = blockIdx.x * B + c;
   const int ky = blockIdx.y;
-  const bool ok = col < ncols;
+  const bool ok = col < ncols && t < G::T;
   const long long zs = (long long)ny * pitch;
   const long long off = (long long)ky * pitch + col;
   float2 v[kVals];

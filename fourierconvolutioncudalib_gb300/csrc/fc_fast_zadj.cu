@@ -1,0 +1,64 @@
+// Register-resident fused z passes of the adjoint: the conjugate-kernel
+// product (image gradient) and the kernel-gradient correlation
+// (templates in fc_fast_cols.cuh).
+#include "fc_fast_cols.cuh"
+
+namespace fc {
+namespace fast {
+// opt in to more than 48 KiB of dynamic shared memory where a kernel needs it
+template <class K>
+static cudaError_t set_dyn_smem(K kernel, int bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <bool CONJ>
+static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+                                float scale, const FcAxis& az, cudaStream_t st) {
+  if (ny <= 0 || ncols <= 0) return cudaSuccess;
+  switch (az.n) {
+#define FC_CASE(n_)                                                                                             \
+  case n_: {                                                                                                    \
+    using G = ColGeom<n_>;                                                                                      \
+    constexpr int sm = ZGeom<n_>::SMEM_BYTES;                                                                   \
+    dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                   \
+    const cudaError_t e = set_dyn_smem(k_zconv<n_, CONJ>, sm);                                                  \
+    if (e != cudaSuccess) return e;                                                                             \
+    k_zconv<n_, CONJ><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W);        \
+    return cudaGetLastError();                                                                                  \
+  }
+    FC_COL_SIZES(FC_CASE)
+#undef FC_CASE
+    default:
+      return cudaErrorNotSupported;
+  }
+}
+}  // namespace fast
+
+cudaError_t fast_zconv_conj(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+                            float scale, const FcAxis& az, cudaStream_t st) {
+  return fast::zconv_launch<true>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az, st);
+}
+
+cudaError_t fast_zcorr(const float2* X, const float2* G_, float2* out, long long pitch, int ny, int ncols, int kz,
+                       int hz, float scale, const FcAxis& az, cudaStream_t st) {
+  if (ny <= 0 || ncols <= 0) return cudaSuccess;
+  switch (az.n) {
+#define FC_CASE(n_)                                                                                          \
+  case n_: {                                                                                                 \
+    using G = fast::ColGeom<n_>;                                                                             \
+    constexpr int sm = fast::ZGeom<n_>::SMEM_BYTES;                                                          \
+    dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                \
+    const cudaError_t e = fast::set_dyn_smem(fast::k_zcorr<n_>, sm);                                         \
+    if (e != cudaSuccess) return e;                                                                          \
+    fast::k_zcorr<n_><<<grid, G::THREADS, sm, st>>>(X, G_, out, pitch, ny, ncols, kz, hz, scale, az.W);       \
+    return cudaGetLastError();                                                                               \
+  }
+    FC_COL_SIZES(FC_CASE)
+#undef FC_CASE
+    default:
+      return cudaErrorNotSupported;
+  }
+}
+
+}  // namespace fc

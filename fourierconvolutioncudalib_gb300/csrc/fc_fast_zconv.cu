@@ -1,5 +1,6 @@
-// Register-resident fused z passes (convolution and kernel gradient):
-// instantiations and launchers (templates in fc_fast_cols.cuh).
+// Register-resident fused z pass of the convolution (kernel spectrum as is):
+// instantiations and launcher (templates in fc_fast_cols.cuh; the
+// conjugate-kernel and kernel-gradient variants are in fc_fast_zadj.cu).
 #include "fc_fast_cols.cuh"
 
 namespace fc {
@@ -10,27 +11,20 @@ static cudaError_t set_dyn_smem(K kernel, int bytes) {
   if (bytes <= 48 * 1024) return cudaSuccess;
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
-}  // namespace fast
 
-cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
-                       float scale, bool conj_kernel, const FcAxis& az, cudaStream_t st) {
+template <bool CONJ>
+static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+                                float scale, const FcAxis& az, cudaStream_t st) {
   if (ny <= 0 || ncols <= 0) return cudaSuccess;
   switch (az.n) {
 #define FC_CASE(n_)                                                                                             \
   case n_: {                                                                                                    \
-    using G = fast::ColGeom<n_>;                                                                                \
-    constexpr int sm = fast::ZGeom<n_>::SMEM_BYTES;                                                             \
+    using G = ColGeom<n_>;                                                                                      \
+    constexpr int sm = ZGeom<n_>::SMEM_BYTES;                                                                   \
     dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                   \
-    cudaError_t e;                                                                                              \
-    if (conj_kernel) {                                                                                          \
-      e = fast::set_dyn_smem(fast::k_zconv<n_, true>, sm);                                                      \
-      if (e != cudaSuccess) return e;                                                                           \
-      fast::k_zconv<n_, true><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W);   \
-    } else {                                                                                                    \
-      e = fast::set_dyn_smem(fast::k_zconv<n_, false>, sm);                                                     \
-      if (e != cudaSuccess) return e;                                                                           \
-      fast::k_zconv<n_, false><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W);  \
-    }                                                                                                           \
+    const cudaError_t e = set_dyn_smem(k_zconv<n_, CONJ>, sm);                                                  \
+    if (e != cudaSuccess) return e;                                                                             \
+    k_zconv<n_, CONJ><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W);        \
     return cudaGetLastError();                                                                                  \
   }
     FC_COL_SIZES(FC_CASE)
@@ -39,26 +33,15 @@ cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, in
       return cudaErrorNotSupported;
   }
 }
+}  // namespace fast
 
-cudaError_t fast_zcorr(const float2* X, const float2* G_, float2* out, long long pitch, int ny, int ncols, int kz,
-                       int hz, float scale, const FcAxis& az, cudaStream_t st) {
-  if (ny <= 0 || ncols <= 0) return cudaSuccess;
-  switch (az.n) {
-#define FC_CASE(n_)                                                                                          \
-  case n_: {                                                                                                 \
-    using G = fast::ColGeom<n_>;                                                                             \
-    constexpr int sm = fast::ZGeom<n_>::SMEM_BYTES;                                                          \
-    dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                \
-    const cudaError_t e = fast::set_dyn_smem(fast::k_zcorr<n_>, sm);                                         \
-    if (e != cudaSuccess) return e;                                                                          \
-    fast::k_zcorr<n_><<<grid, G::THREADS, sm, st>>>(X, G_, out, pitch, ny, ncols, kz, hz, scale, az.W);       \
-    return cudaGetLastError();                                                                               \
-  }
-    FC_COL_SIZES(FC_CASE)
-#undef FC_CASE
-    default:
-      return cudaErrorNotSupported;
-  }
+cudaError_t fast_zconv_conj(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+                            float scale, const FcAxis& az, cudaStream_t st);
+
+cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
+                       float scale, bool conj_kernel, const FcAxis& az, cudaStream_t st) {
+  if (conj_kernel) return fast_zconv_conj(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az, st);
+  return fast::zconv_launch<false>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az, st);
 }
 
 }  // namespace fc

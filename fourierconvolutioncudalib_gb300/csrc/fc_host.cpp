@@ -12,7 +12,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <fstream>
+#include <sstream>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -23,7 +26,10 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "../../include/convolution3Dfft.h"
+#include "fc_batched.cuh"
 #include "fc_internal.h"
 
 namespace fc {
@@ -741,6 +747,470 @@ static void dims3(const int* d, int* a, int* b, int* cc) {
   *cc = d[2];
 }
 
+// ------------------------------------------------------------------ batched convolution
+// Many volumes of uneven sizes, each with its own kernel.  Views whose three
+// axis lengths all have register-resident kernels run as five passes over the
+// whole batch -- x R2C (kernels and images), y forward (kernels and images),
+// fused z, y inverse, x C2R -- each pass one persistent launch over a device
+// work-list (BTask, fc_batched.cuh) or, where the tuner measured it faster,
+// one launch per view.  Other views run the single-volume sequence.  The
+// whole sequence is captured once per call signature (shapes, pointers,
+// workspace, stream) into a CUDA graph and replayed.
+
+enum BChoice : int { kFatOcc = 0, kFatOne = 1, kPerView = 2 };
+static const char* const kBPassName[5] = {"batch_x_r2c", "batch_y_fwd", "batch_zconv", "batch_y_inv", "batch_x_c2r"};
+
+struct BatchEntry {
+  std::vector<BTask> tasks[5];
+  long long total[5] = {0, 0, 0, 0, 0};
+  size_t smem[5] = {0, 0, 0, 0, 0};
+  double bytes[5] = {0, 0, 0, 0, 0};
+  std::vector<int> slow_views;
+  std::vector<Geom> g;
+  std::vector<size_t> off;
+  BTask* d_tasks = nullptr;
+  size_t task_off[5] = {0, 0, 0, 0, 0};
+  int choice[5] = {kFatOcc, kFatOcc, kFatOcc, kFatOcc, kFatOcc};
+  bool view_major = false;  // run each view's five passes in turn (its spectra stay in L2)
+  std::vector<std::vector<std::pair<int, int>>> view_tasks;  // per fast view: (pass, task index)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~BatchEntry() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (d_tasks) cudaFree(d_tasks);
+  }
+};
+
+static std::mutex g_batch_mu;
+static std::map<std::string, std::unique_ptr<BatchEntry>> g_batch;
+static int g_use_graphs = -1;
+static bool use_graphs() {
+  if (g_use_graphs < 0) {
+    const char* e = std::getenv("FC_GRAPH");
+    g_use_graphs = (e && std::atoi(e) == 0) ? 0 : 1;
+  }
+  return g_use_graphs == 1;
+}
+
+static FcAxis task_axis(const BTask& t) {
+  FcAxis a;
+  std::memset(&a, 0, sizeof(a));
+  a.n = t.n;
+  a.W = t.W;
+  return a;
+}
+
+// one view's tasks of the five passes
+static void add_view_tasks(BatchEntry& E, const Geom& g, const Axes& a, const float* img, float* out,
+                           const float* taps, char* w, const Layout& L) {
+  float2* S = (float2*)(w + L.off_S);
+  float2* KX = (float2*)(w + L.off_KX);
+  float2* KXY = (float2*)(w + L.off_KXY);
+  const long long rows = (long long)g.ny * g.nz;
+  const double mc = 8.0 * g.nxh * (double)rows;
+  auto mk = [](int mode, int n, const float2* W) {
+    BTask t;
+    std::memset(&t, 0, sizeof(t));
+    t.mode = mode;
+    t.n = n;
+    t.W = W;
+    return t;
+  };
+  // x R2C: kernel taps (box) and image
+  BTask kx = mk(kBRowsBox, g.nx, a.x.W);
+  kx.rows = (long long)g.kplanes * g.krows;
+  kx.src = taps;
+  kx.dst = KX;
+  kx.p1 = g.pitch;
+  kx.i0 = g.kx;
+  kx.i1 = g.kx / 2;
+  kx.tiles = batched_row_tiles(g.nx, kx.rows);
+  BTask ix = mk(kBRowsDense, g.nx, a.x.W);
+  ix.rows = rows;
+  ix.src = img;
+  ix.p0 = g.nx;
+  ix.dst = S;
+  ix.p1 = g.pitch;
+  ix.tiles = batched_row_tiles(g.nx, rows);
+  E.tasks[0].push_back(kx);
+  E.tasks[0].push_back(ix);
+  E.bytes[0] += 4.0 * g.kx * kx.rows + 8.0 * g.nxh * kx.rows + 4.0 * g.N() + mc;
+  // y forward: kernel (from the compact x-spectrum rows) and image
+  BTask ky = mk(kBColsKX, g.ny, a.y.W);
+  ky.src = KX;
+  ky.dst = KXY;
+  ky.p0 = (long long)g.ny * g.pitch;
+  ky.p1 = g.pitch;
+  ky.i0 = g.krows;
+  ky.i1 = g.ky / 2;
+  ky.ncols = g.nxh;
+  ky.rows = g.kplanes;
+  ky.tiles = batched_col_tiles(g.ny, g.nxh, g.kplanes);
+  BTask iy = mk(kBColsFwd, g.ny, a.y.W);
+  iy.dst = S;
+  iy.p0 = (long long)g.ny * g.pitch;
+  iy.p1 = g.pitch;
+  iy.ncols = g.nxh;
+  iy.rows = g.nz;
+  iy.tiles = batched_col_tiles(g.ny, g.nxh, g.nz);
+  E.tasks[1].push_back(ky);
+  E.tasks[1].push_back(iy);
+  E.bytes[1] += 8.0 * g.nxh * ((double)g.krows * g.kplanes + (double)g.ny * g.kplanes) + 2.0 * mc;
+  // fused z
+  BTask z = mk(kBZconv, g.nz, a.z.W);
+  z.dst = S;
+  z.aux = KXY;
+  z.p0 = g.pitch;
+  z.rows = g.ny;
+  z.ncols = g.nxh;
+  z.i0 = g.kplanes;
+  z.i1 = g.kz / 2;
+  z.scale = 1.0f / (float)g.N();
+  z.tiles = batched_col_tiles(g.nz, g.nxh, g.ny);
+  E.tasks[2].push_back(z);
+  E.bytes[2] += 2.0 * mc + 8.0 * g.nxh * (double)g.ny * g.kplanes;
+  // y inverse
+  BTask yi = iy;
+  yi.mode = kBColsInv;
+  E.tasks[3].push_back(yi);
+  E.bytes[3] += 2.0 * mc;
+  // x C2R
+  BTask xc = mk(kBRowsC2R, g.nx, a.x.W);
+  xc.rows = rows;
+  xc.src = S;
+  xc.p0 = g.pitch;
+  xc.dst = out;
+  xc.p1 = g.nx;
+  xc.tiles = ix.tiles;
+  E.tasks[4].push_back(xc);
+  E.bytes[4] += mc + 4.0 * g.N();
+}
+
+static int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    n = 1;
+  }
+  return n;
+}
+
+static void launch_task(const BTask& t, int p, cudaStream_t st);
+
+static void launch_pass(BatchEntry& E, int p, int choice, cudaStream_t st) {
+  const std::vector<BTask>& T = E.tasks[p];
+  if (T.empty()) return;
+  if (choice == kPerView) {
+    for (const BTask& t : T) launch_task(t, p, st);
+    return;
+  }
+  const BTask* d = E.d_tasks + E.task_off[p];
+  const int nt = (int)T.size();
+  int occ = 1;
+  switch (p) {
+    case 0: occ = batched_occupancy_rows_fwd(E.smem[p]); break;
+    case 1: occ = batched_occupancy_cols_fwd(E.smem[p]); break;
+    case 2: occ = batched_occupancy_zconv(E.smem[p]); break;
+    case 3: occ = batched_occupancy_cols_inv(E.smem[p]); break;
+    default: occ = batched_occupancy_rows_inv(E.smem[p]); break;
+  }
+  const long long want = (long long)sm_count() * (choice == kFatOne ? 1 : occ);
+  const int grid = (int)std::max<long long>(1, std::min<long long>(want, E.total[p]));
+  cudaError_t e;
+  switch (p) {
+    case 0: e = batched_rows_fwd(d, nt, E.total[p], grid, E.smem[p], st); break;
+    case 1: e = batched_cols_fwd(d, nt, E.total[p], grid, E.smem[p], st); break;
+    case 2: e = batched_zconv(d, nt, E.total[p], grid, E.smem[p], st); break;
+    case 3: e = batched_cols_inv(d, nt, E.total[p], grid, E.smem[p], st); break;
+    default: e = batched_rows_inv(d, nt, E.total[p], grid, E.smem[p], st); break;
+  }
+  cuda_check(e, kBPassName[p]);
+  ++t_launches;
+}
+
+// one task on the single-volume kernel of its length
+static void launch_task(const BTask& t, int p, cudaStream_t st) {
+  const FcAxis ax = task_axis(t);
+  cudaError_t e = cudaSuccess;
+  switch (t.mode) {
+    case kBRowsBox:
+      e = fast_x_r2c_box((const float*)t.src, t.i0, t.i1, (float2*)t.dst, t.p1, t.rows, ax, st);
+      break;
+    case kBRowsDense:
+      e = fast_x_r2c_dense((const float*)t.src, t.p0, (float2*)t.dst, t.p1, t.rows, ax, st);
+      break;
+    case kBRowsC2R:
+      e = fast_x_c2r((const float2*)t.src, t.p0, (float*)t.dst, t.p1, t.rows, ax, st);
+      break;
+    case kBColsKX:
+      e = fast_cols_kx((const float2*)t.src, t.p1, t.i0, t.i1, (float2*)t.dst, t.ncols, (int)t.rows, ax, st);
+      break;
+    case kBColsFwd:
+    case kBColsInv:
+      e = fast_cols((float2*)t.dst, (float2*)t.dst, t.p0, t.p1, t.ncols, (int)t.rows, t.mode == kBColsInv, ax,
+                    st);
+      break;
+    case kBZconv:
+      e = fast_zconv((float2*)t.dst, (const float2*)t.aux, t.p0, (int)t.rows, t.ncols, t.i0, t.i1, t.scale, false,
+                     ax, st);
+      break;
+    default:
+      break;
+  }
+  cuda_check(e, kBPassName[p]);
+  ++t_launches;
+}
+
+static void run_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, float* const* outs,
+                      const float* const* kers, char* ws, cudaStream_t st) {
+  if (E.view_major) {
+    for (const auto& vt : E.view_tasks)
+      for (const auto& pt : vt) launch_task(E.tasks[pt.first][pt.second], pt.first, st);
+  } else {
+    for (int p = 0; p < 5; ++p) {
+      PassScope ps(kBPassName[p], E.bytes[p], st);
+      launch_pass(E, p, E.choice[p], st);
+    }
+  }
+  for (int v : E.slow_views)
+    enqueue_conv(c, E.g[v], imgs[v], outs[v], kers[v], false, ws + E.off[v], plain_layout(E.g[v], false).total, st);
+}
+
+// ---- tuner: per pass, the fastest of {persistent launch at full occupancy,
+// persistent launch with one CTA per SM, one launch per view}, then the
+// faster of that pass-major schedule and the view-major one, measured with
+// CUDA events on the first call of a new (GPU, view shapes) signature and
+// cached in memory and in FC_TUNE_CACHE (default ~/.cache/fc_gb300_tune.txt);
+// FC_AUTOTUNE=0 keeps the persistent launches untimed, FC_TUNE_LOG=1 prints
+// the measurements.
+static std::string tune_path() {
+  const char* e = std::getenv("FC_TUNE_CACHE");
+  if (e && *e) return e;
+  const char* h = std::getenv("HOME");
+  return std::string(h ? h : ".") + "/.cache/fc_gb300_tune.txt";
+}
+
+static bool tune_lookup(const std::string& sig, int* choice, bool* view_major) {
+  std::ifstream f(tune_path());
+  std::string line;
+  while (std::getline(f, line)) {
+    std::istringstream is(line);
+    std::string k;
+    int ch[6];
+    if (!(is >> k)) continue;
+    if (k != sig) continue;
+    bool ok = true;
+    for (int i = 0; i < 6; ++i) ok = ok && (bool)(is >> ch[i]);
+    if (!ok) continue;
+    for (int i = 0; i < 5; ++i) choice[i] = ch[i];
+    *view_major = ch[5] != 0;
+    return true;
+  }
+  return false;
+}
+
+static void tune_store(const std::string& sig, const int* choice, bool view_major) {
+  const std::string path = tune_path();
+  const size_t slash = path.find_last_of('/');
+  if (slash != std::string::npos) {
+    const std::string dir = path.substr(0, slash);
+    std::string cmd;  // create the directory without a shell: walk the components
+    for (size_t i = 1; i <= dir.size(); ++i)
+      if (i == dir.size() || dir[i] == '/') {
+        const std::string part = dir.substr(0, i);
+        mkdir(part.c_str(), 0755);
+      }
+  }
+  std::ofstream f(path, std::ios::app);
+  if (!f) return;
+  f << sig;
+  for (int i = 0; i < 5; ++i) f << ' ' << choice[i];
+  f << ' ' << (view_major ? 1 : 0) << '\n';
+}
+
+// on unless FC_AUTOTUNE=0
+static bool autotune_enabled() {
+  const char* e = std::getenv("FC_AUTOTUNE");
+  return !e || std::atoi(e) != 0;
+}
+static bool tune_log() {
+  const char* e = std::getenv("FC_TUNE_LOG");
+  return e && std::atoi(e) != 0;
+}
+
+static void autotune_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, float* const* outs,
+                           const float* const* kers, char* ws, cudaStream_t st) {
+  cudaEvent_t a, b;
+  cuda_check(cudaEventCreate(&a), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&b), "cudaEventCreate");
+  run_batch(c, E, imgs, outs, kers, ws, st);  // warm: every kernel loaded, caches primed
+  for (int p = 0; p < 5; ++p) {
+    if (E.tasks[p].empty()) continue;
+    float best = 1e30f;
+    int best_choice = E.choice[p];
+    for (int ch = 0; ch < 3; ++ch) {
+      float tmin = 1e30f;
+      for (int r = 0; r < 4; ++r) {
+        cuda_check(cudaEventRecord(a, st), "cudaEventRecord");
+        launch_pass(E, p, ch, st);
+        cuda_check(cudaEventRecord(b, st), "cudaEventRecord");
+        cuda_check(cudaEventSynchronize(b), "cudaEventSynchronize");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (r > 0) tmin = std::min(tmin, ms);
+      }
+      if (tune_log()) std::fprintf(stderr, "fc tune %s choice %d: %.1f us\n", kBPassName[p], ch, 1e3 * tmin);
+      if (tmin < best) {
+        best = tmin;
+        best_choice = ch;
+      }
+    }
+    E.choice[p] = best_choice;
+  }
+  // whole batch: the tuned pass-major schedule against the view-major one
+  float t_sched[2] = {1e30f, 1e30f};
+  for (int vm = 0; vm < 2; ++vm) {
+    E.view_major = vm == 1;
+    for (int r = 0; r < 4; ++r) {
+      cuda_check(cudaEventRecord(a, st), "cudaEventRecord");
+      run_batch(c, E, imgs, outs, kers, ws, st);
+      cuda_check(cudaEventRecord(b, st), "cudaEventRecord");
+      cuda_check(cudaEventSynchronize(b), "cudaEventSynchronize");
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (r > 0) t_sched[vm] = std::min(t_sched[vm], ms);
+    }
+    if (tune_log()) std::fprintf(stderr, "fc tune schedule %s: %.1f us\n", vm ? "view-major" : "pass-major",
+                                 1e3 * t_sched[vm]);
+  }
+  E.view_major = t_sched[1] < t_sched[0];
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+}
+
+static std::string batch_signature(int nv, const int* dims) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp prop;
+  std::string name = "gpu";
+  if (cudaGetDeviceProperties(&prop, dev) == cudaSuccess) name = prop.name;
+  for (char& ch : name)
+    if (ch == ' ') ch = '_';
+  std::ostringstream os;
+  os << name << ":v1";
+  for (int i = 0; i < 6 * nv; ++i) os << (i % 6 == 0 ? ':' : 'x') << dims[i];
+  return os.str();
+}
+
+static void enqueue_batched(DevCtx& c, int nv, const float* const* imgs, float* const* outs,
+                            const float* const* kers, const int* dims, bool compat, char* ws, size_t wsb,
+                            cudaStream_t st) {
+  // key: shapes, pointers, workspace, stream, device
+  std::ostringstream ks;
+  ks << c.dev << '|' << (const void*)st << '|' << (const void*)ws << '|' << compat;
+  for (int v = 0; v < nv; ++v) {
+    for (int i = 0; i < 6; ++i) ks << ',' << dims[6 * v + i];
+    ks << '|' << (const void*)imgs[v] << (const void*)outs[v] << (const void*)kers[v];
+  }
+  const std::string key = ks.str();
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  auto it = g_batch.find(key);
+  BatchEntry* E = nullptr;
+  if (it == g_batch.end() && g_batch.size() >= 32) {
+    // bounded cache: drop every entry once 32 signatures have accumulated
+    cudaStreamSynchronize(st);
+    g_batch.clear();
+  }
+  if (it == g_batch.end()) {
+    auto e = std::make_unique<BatchEntry>();
+    size_t off = 0;
+    for (int v = 0; v < nv; ++v) {
+      const int* d = dims + 6 * v;
+      const Geom g = make_geom(d[0], d[1], d[2], d[3], d[4], d[5], false);
+      const Layout L = conv_layout(g, false);
+      e->g.push_back(g);
+      e->off.push_back(off);
+      const Axes a = axes_for(c, g);  // twiddles exist before any capture
+      const bool fast = !compat && use_fast() && fast_rows_supported(g.nx) && fast_cols_supported(g.ny) &&
+                        fast_cols_supported(g.nz);
+      if (fast) {
+        size_t before[5];
+        for (int p = 0; p < 5; ++p) before[p] = e->tasks[p].size();
+        add_view_tasks(*e, g, a, imgs[v], outs[v], kers[v], ws + off, L);
+        std::vector<std::pair<int, int>> mine;
+        for (int p = 0; p < 5; ++p)
+          for (size_t i = before[p]; i < e->tasks[p].size(); ++i) mine.push_back({p, (int)i});
+        e->view_tasks.push_back(mine);
+      } else {
+        e->slow_views.push_back(v);
+      }
+      off += plain_layout(g, compat).total;
+    }
+    if (off > wsb) FC_THROW(FC_ERR_NOMEM, "workspace too small");
+    size_t ntask = 0;
+    for (int p = 0; p < 5; ++p) {
+      long long t0 = 0;
+      size_t sm = 0;
+      for (BTask& t : e->tasks[p]) {
+        t.tile0 = t0;
+        t0 += t.tiles;
+        size_t need = (p == 0 || p == 4) ? batched_row_smem(t.n) : batched_col_smem(t.n, p == 2);
+        sm = std::max(sm, need);
+      }
+      if (p == 2) sm += sizeof(float2) * kBatchThreads * 16;
+      e->total[p] = t0;
+      e->smem[p] = sm;
+      e->task_off[p] = ntask;
+      ntask += e->tasks[p].size();
+    }
+    if (ntask) {
+      std::vector<BTask> all;
+      for (int p = 0; p < 5; ++p) all.insert(all.end(), e->tasks[p].begin(), e->tasks[p].end());
+      cuda_check(cudaMalloc(&e->d_tasks, sizeof(BTask) * ntask), "cudaMalloc(work-list)");
+      cuda_check(cudaMemcpy(e->d_tasks, all.data(), sizeof(BTask) * ntask, cudaMemcpyHostToDevice),
+                 "cudaMemcpy(work-list)");
+    }
+    const std::string sig = batch_signature(nv, dims);
+    if (!tune_lookup(sig, e->choice, &e->view_major) && autotune_enabled()) {
+      autotune_batch(c, *e, imgs, outs, kers, ws, st);
+      tune_store(sig, e->choice, e->view_major);
+    }
+    E = e.get();
+    g_batch[key] = std::move(e);
+  } else {
+    E = it->second.get();
+  }
+  if (!use_graphs() || g_prof_on) {
+    run_batch(c, *E, imgs, outs, kers, ws, st);
+    return;
+  }
+  if (!E->exec) {
+    // capture on the library's own stream (the caller's may be the legacy
+    // default stream, which cannot be captured); the graph is then launched
+    // on the caller's stream
+    struct NoEvents {
+      NoEvents() { t_no_events = true; }
+      ~NoEvents() { t_no_events = false; }
+    } no_events;
+    cudaStream_t cs = ctx_stream(c);
+    cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    try {
+      run_batch(c, *E, imgs, outs, kers, ws, cs);
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(cs, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    cuda_check(cudaStreamEndCapture(cs, &E->graph), "cudaStreamEndCapture");
+    cuda_check(cudaGraphInstantiate(&E->exec, E->graph, 0), "cudaGraphInstantiate");
+  }
+  cuda_check(cudaGraphLaunch(E->exec, st), "cudaGraphLaunch");
+  t_launches += 1;
+}
+
 // ------------------------------------------------------------------ scratch-only convolution
 // Used by the allocation-free entry point (fc_noalloc.cu).  Layout of the
 // scratch: the three twiddle tables, then the convolution workspace.
@@ -1144,12 +1614,7 @@ int fc_conv3d_batched_device(int n_views, const float* const* d_images, float* c
     std::lock_guard<std::mutex> lk(c.mu);
     size_t wsb = workspace_bytes;
     char* ws = (char*)resolve_ws(c, d_workspace, &wsb, need);
-    size_t off = 0;
-    for (int v = 0; v < n_views; ++v) {
-      const size_t b = plain_layout(gs[v], compat).total;
-      enqueue_conv(c, gs[v], d_images[v], d_outs[v], d_kernels[v], compat, ws + off, b, (cudaStream_t)stream);
-      off += b;
-    }
+    enqueue_batched(c, n_views, d_images, d_outs, d_kernels, dims, compat, ws, wsb, (cudaStream_t)stream);
   });
 }
 
