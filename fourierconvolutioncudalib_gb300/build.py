@@ -23,9 +23,12 @@ LIB_PATH = PKG / LIB_NAME
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", str(ROOT / "include")]
-SOURCES = ["fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu", "fc_fast_zconv.cu", "fc_fast_zadj.cu",
-           "fc_batched_rows_fwd.cu", "fc_batched_rows_inv.cu", "fc_batched_cols_fwd.cu", "fc_batched_cols_inv.cu",
-           "fc_batched_zconv.cu", "fc_noalloc.cu"]
+# (source, object name, extra flags); fc_tc.cu is built once per 16-bit operand type
+SOURCES = [(f, Path(f).stem, []) for f in [
+    "fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu", "fc_fast_zconv.cu", "fc_fast_zadj.cu",
+    "fc_batched_rows_fwd.cu", "fc_batched_rows_inv.cu", "fc_batched_cols_fwd.cu", "fc_batched_cols_inv.cu",
+    "fc_batched_zconv.cu", "fc_noalloc.cu"]] + [
+    ("fc_tc.cu", "fc_tc_fp16", ["-DFC_TC_MODE=1"]), ("fc_tc.cu", "fc_tc_bf16", ["-DFC_TC_MODE=2"])]
 
 
 def nvcc() -> str:
@@ -40,10 +43,11 @@ def _sources_mtime() -> float:
     return max(f.stat().st_mtime for f in files if f.is_file())
 
 
-def _compile(src: str, verbose: bool) -> Path:
-    obj = BUILD / (Path(src).stem + ".o")
+def _compile(entry, verbose: bool) -> Path:
+    src, stem, flags = entry
+    obj = BUILD / (stem + ".o")
     extra = os.environ.get("FC_NVCC_EXTRA", "").split()  # e.g. -DFC_ZCONV_MIN_BLOCKS=3 for tuning builds
-    cmd = [nvcc(), *COMMON, *ARCH, *extra, "-c", str(CSRC / src), "-o", str(obj)]
+    cmd = [nvcc(), *COMMON, *ARCH, *flags, *extra, "-c", str(CSRC / src), "-o", str(obj)]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -59,7 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     workers = min(len(SOURCES), os.cpu_count() or 4)
     # longest translation units first
-    order = sorted(SOURCES, key=lambda f: 0 if f.startswith(("fc_batched", "fc_fast_z")) else 1)
+    order = sorted(SOURCES, key=lambda e: 0 if e[0].startswith(("fc_batched", "fc_fast_z", "fc_tc")) else 1)
     with ThreadPoolExecutor(max_workers=workers) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), order))
     tmp = BUILD / (LIB_NAME + ".tmp")

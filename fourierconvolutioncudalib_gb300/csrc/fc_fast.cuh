@@ -20,11 +20,18 @@
 //     between a forward and an inverse transform happens in registers.
 #pragma once
 #include "fc_fft.cuh"
+#include "fc_tc.cuh"
 
 namespace fc {
 namespace fast {
 
 constexpr int kVals = 16;  // values per thread
+
+// tensor-core mode context: per-warp scratch and the CTA's A-fragment table
+struct TcCtx {
+  uint32_t* ws;
+  const uint32_t* tab;
+};
 
 __host__ __device__ constexpr int pick_radix(int rem) {
   return rem % 16 == 0   ? 16
@@ -103,8 +110,9 @@ struct ColLay {
   }
 };
 
-template <int N, int R, int NS, bool INV>
-__device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const float2* __restrict__ W) {
+template <int N, int R, int NS, bool INV, int TCM>
+__device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const float2* __restrict__ W,
+                                      const TcCtx& tcx) {
   constexpr int U = kVals / R;
   constexpr int A = Plan<N>::A(R);
   constexpr int NB = N / R;
@@ -118,9 +126,13 @@ __device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const flo
 #pragma unroll
       for (int r = 1; r < R; ++r) v[b * R + r] = c_tw<INV>(v[b * R + r], __ldg(W + k * r * TWS));
     }
-    Dft<R, INV>::run(&v[b * R]);
+    if constexpr (TCM != tc::kNone && R == 16)
+      tc::dft16<INV, TCM>(&v[b * R], tcx.ws, tcx.tab);
+    else
+      Dft<R, INV>::run(&v[b * R]);
   }
   (void)NB;
+  (void)tcx;
 }
 
 template <int N, int R, int NS, int R2, class L>
@@ -150,25 +162,27 @@ __device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const 
 }
 
 // stages I .. S-1 of the forward chain (INV = false) or of the reversed chain (INV = true)
-template <int N, int I, int NS, bool INV>
+template <int N, int I, int NS, bool INV, int TCM>
 struct Chain {
   template <class L>
   static __device__ __forceinline__ void run(float2 (&v)[kVals], const L& sm, const int t,
-                                             const float2* __restrict__ W) {
+                                             const float2* __restrict__ W, const TcCtx& tcx) {
     constexpr int R = Plan<N>::radix(I, INV);
-    stage<N, R, NS, INV>(v, t, W);
+    stage<N, R, NS, INV, TCM>(v, t, W, tcx);
     if constexpr (I + 1 < Plan<N>::S) {
       constexpr int R2 = Plan<N>::radix(I + 1, INV);
       exchange<N, R, NS, R2>(v, sm, t);
-      Chain<N, I + 1, NS * R, INV>::run(v, sm, t, W);
+      Chain<N, I + 1, NS * R, INV, TCM>::run(v, sm, t, W, tcx);
     }
   }
 };
 
-// full transform; inputs per first_pos, outputs per last_pos
-template <int N, bool INV, class L>
-__device__ __forceinline__ void fft(float2 (&v)[kVals], const L& sm, const int t, const float2* __restrict__ W) {
-  Chain<N, 0, 1, INV>::run(v, sm, t, W);
+// full transform; inputs per first_pos, outputs per last_pos.  TCM selects
+// the tensor-core 16-point DFT for the radix-16 stages (tc::kFp16 / kBf16).
+template <int N, bool INV, int TCM = tc::kNone, class L>
+__device__ __forceinline__ void fft(float2 (&v)[kVals], const L& sm, const int t, const float2* __restrict__ W,
+                                    const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+  Chain<N, 0, 1, INV, TCM>::run(v, sm, t, W, tcx);
 }
 
 // radix of the first / last stage of the forward (INV=false) or inverse chain

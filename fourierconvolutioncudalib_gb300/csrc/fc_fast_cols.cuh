@@ -33,9 +33,10 @@ struct ColGeom {
 };
 
 // y pass body: tile (bx, plane) = columns [bx*B, bx*B + B) of one plane.
-template <int N, bool INV, class Src>
+template <int N, bool INV, class Src, int TCM = tc::kNone>
 __device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long ps, long long es, int ncols,
-                                          const float2* __restrict__ W, int bx, int plane, int tid, float2* sm) {
+                                          const float2* __restrict__ W, int bx, int plane, int tid, float2* sm,
+                                          const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
   using G = ColGeom<N>;
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, INV>(), RF = last_radix<N, INV>();
@@ -49,7 +50,7 @@ __device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long
     const int j = stage_pos<N, R0>(t, q);
     v[q] = (ok && j >= 0) ? src.load(plane, j, col) : make_float2(0.f, 0.f);
   }
-  fft<N, INV>(v, ColLay<B>{sm, c}, t, W);
+  fft<N, INV, TCM>(v, ColLay<B>{sm, c}, t, W, tcx);
   if (ok) {
     float2* d = dst + (long long)plane * ps + col;
 #pragma unroll
@@ -79,11 +80,11 @@ struct ZGeom {
 };
 
 // fused z pass body: tile (bx, ky); stash holds nstash >= THREADS slots per value index
-template <int N, bool CONJ>
+template <int N, bool CONJ, int TCM = tc::kNone>
 __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch,
                                            int ny, int ncols, int kplanes, int hz, float scale,
                                            const float2* __restrict__ W, int bx, int ky, int tid, float2* sm,
-                                           float2* stash, int nstash) {
+                                           float2* stash, int nstash, const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
   using G = ColGeom<N>;
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, false>(), RF = last_radix<N, true>();
@@ -102,7 +103,7 @@ __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2*
     if (p >= N) p -= N;
     v[q] = (ok && z >= 0 && p < kplanes) ? KXY[((long long)p * ny + ky) * pitch + col] : make_float2(0.f, 0.f);
   }
-  fft<N, false>(v, lay, t, W);
+  fft<N, false, TCM>(v, lay, t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) stash[q * nstash + tid] = v[q];
 #pragma unroll
@@ -110,7 +111,7 @@ __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2*
     const int z = stage_pos<N, R0>(t, q);
     v[q] = (ok && z >= 0) ? base[z * zs] : make_float2(0.f, 0.f);
   }
-  fft<N, false>(v, lay, t, W);
+  fft<N, false, TCM>(v, lay, t, W, tcx);
   // the forward outputs sit where the inverse's first stage reads them
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
@@ -119,7 +120,7 @@ __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2*
     if (CONJ) a.y = -a.y;
     v[q] = make_float2(scale * (a.x * b.x - a.y * b.y), scale * (a.y * b.x + a.x * b.y));
   }
-  fft<N, true>(v, lay, t, W);
+  fft<N, true, TCM>(v, lay, t, W, tcx);
   if (ok) {
 #pragma unroll
     for (int q = 0; q < kVals; ++q) {

@@ -1,6 +1,6 @@
 // Register-resident x-pass bodies (R2C / C2R) for row lengths in FC_ROW_SIZES,
 // shared by the single-volume kernels (fc_fast_rows.cu) and the batched
-// persistent kernels (fc_batched.cu).
+// persistent kernels (fc_batched_rows_fwd.cu, fc_batched_rows_inv.cu).
 //
 // Two real rows a, b are transformed as one complex line z = a + i b.  A line
 // is held by T = Plan<N>::T threads; a tile is LPB = max(1, 256/T) lines
@@ -28,10 +28,10 @@ struct RowGeom {
   static long long tiles(long long nrows) { return (nrows + 2LL * LPB - 1) / (2LL * LPB); }
 };
 
-template <int N, class Src>
+template <int N, class Src, int TCM = tc::kNone>
 __device__ __forceinline__ void body_r2c(const Src& src, float2* __restrict__ out, long long out_pitch,
                                          long long nrows, const float2* __restrict__ W, long long tile, int tid,
-                                         float2* sm) {
+                                         float2* sm, const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
   using G = RowGeom<N>;
   constexpr int R0 = first_radix<N, false>();
   constexpr int RF = last_radix<N, false>();
@@ -48,7 +48,7 @@ __device__ __forceinline__ void body_r2c(const Src& src, float2* __restrict__ ou
     v[q] = make_float2(0.f, 0.f);
     if (x >= 0) v[q] = make_float2(va ? src.load(ra, x) : 0.f, vb ? src.load(rb, x) : 0.f);
   }
-  fft<N, false>(v, RowLay{lbase}, t, W);
+  fft<N, false, TCM>(v, RowLay{lbase}, t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int x = stage_pos<N, RF>(t, q);
@@ -65,10 +65,11 @@ __device__ __forceinline__ void body_r2c(const Src& src, float2* __restrict__ ou
   }
 }
 
-template <int N>
+template <int N, int TCM = tc::kNone>
 __device__ __forceinline__ void body_c2r(const float2* __restrict__ in, long long in_pitch, float* __restrict__ out,
                                          long long out_pitch, long long nrows, const float2* __restrict__ W,
-                                         long long tile, int tid, float2* sm) {
+                                         long long tile, int tid, float2* sm,
+                                         const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
   using G = RowGeom<N>;
   constexpr int R0 = first_radix<N, true>();
   constexpr int RF = last_radix<N, true>();
@@ -98,7 +99,7 @@ __device__ __forceinline__ void body_c2r(const float2* __restrict__ in, long lon
       v[q] = make_float2(a.x - b.y, a.y + b.x);
     }
   }
-  fft<N, true>(v, RowLay{sm + line * G::LS}, t, W);
+  fft<N, true, TCM>(v, RowLay{sm + line * G::LS}, t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int x = stage_pos<N, RF>(t, q);

@@ -334,33 +334,48 @@ static bool use_fast() {
   return g_generic_only == 0;
 }
 
+// tensor-core mode of the enqueue in progress on this thread: 0 off, 1 fp16, 2 bf16
+static thread_local int t_tc_mode = 0;
+static bool tc_len(int n) { return n == 128 || n == 256 || n == 512 || n == 1024; }
+#define FC_TC_CALL(fn, ...) (t_tc_mode == 1 ? fn##_fp16(__VA_ARGS__) : fn##_bf16(__VA_ARGS__))
+
 static cudaError_t d_x_r2c_dense(const float* in, long long ip, float2* out, long long op, long long rows,
                                  const FcAxis& ax, const Tiles& t, cudaStream_t st) {
+  if (t_tc_mode && tc_len(ax.n)) return FC_TC_CALL(tc_x_r2c, in, ip, nullptr, 0, 0, out, op, rows, ax, st);
   if (use_fast() && fast_rows_supported(ax.n)) return fast_x_r2c_dense(in, ip, out, op, rows, ax, st);
   return launch_x_r2c_dense(in, ip, out, op, rows, ax, t, st);
 }
 static cudaError_t d_x_r2c_box(const float* taps, int kx, int hx, float2* out, long long op, long long rows,
                                const FcAxis& ax, const Tiles& t, cudaStream_t st) {
+  if (t_tc_mode && tc_len(ax.n)) return FC_TC_CALL(tc_x_r2c, nullptr, 0, taps, kx, hx, out, op, rows, ax, st);
   if (use_fast() && fast_rows_supported(ax.n)) return fast_x_r2c_box(taps, kx, hx, out, op, rows, ax, st);
   return launch_x_r2c_box(taps, kx, hx, out, op, rows, ax, t, st);
 }
 static cudaError_t d_x_c2r(const float2* in, long long ip, float* out, long long op, long long rows, const FcAxis& ax,
                            const Tiles& t, cudaStream_t st) {
+  if (t_tc_mode && tc_len(ax.n)) return FC_TC_CALL(tc_x_c2r, in, ip, out, op, rows, ax, st);
   if (use_fast() && fast_rows_supported(ax.n)) return fast_x_c2r(in, ip, out, op, rows, ax, st);
   return launch_x_c2r(in, ip, out, op, rows, ax, t, st);
 }
 static cudaError_t d_cols(const float2* src, float2* dst, long long ps, long long es, int ncols, int nplanes, bool inv,
                           const FcAxis& ax, int cols_log2, int threads, cudaStream_t st) {
+  if (t_tc_mode && tc_len(ax.n))
+    return FC_TC_CALL(tc_cols, inv ? 1 : 0, src, 0, 0, 0, dst, ps, es, ncols, nplanes, ax, st);
   if (use_fast() && fast_cols_supported(ax.n)) return fast_cols(src, dst, ps, es, ncols, nplanes, inv, ax, st);
   return launch_cols(src, dst, ps, es, ncols, nplanes, inv, ax, cols_log2, threads, st);
 }
 static cudaError_t d_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
                              int nplanes, const FcAxis& ax, int cols_log2, int threads, cudaStream_t st) {
+  if (t_tc_mode && tc_len(ax.n))
+    return FC_TC_CALL(tc_cols, 2, kx_spec, pitch, krows, hy, dst, (long long)ax.n * pitch, pitch, ncols, nplanes, ax,
+                      st);
   if (use_fast() && fast_cols_supported(ax.n)) return fast_cols_kx(kx_spec, pitch, krows, hy, dst, ncols, nplanes, ax, st);
   return launch_cols_kx(kx_spec, pitch, krows, hy, dst, ncols, nplanes, ax, cols_log2, threads, st);
 }
 static cudaError_t d_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
                            float scale, bool conj, const FcAxis& az, int cols_log2, int threads, cudaStream_t st) {
+  if (t_tc_mode && !conj && tc_len(az.n))
+    return FC_TC_CALL(tc_zconv, S, KXY, pitch, ny, ncols, kplanes, hz, scale, az, st);
   if (use_fast() && fast_cols_supported(az.n)) return fast_zconv(S, KXY, pitch, ny, ncols, kplanes, hz, scale, conj, az, st);
   return launch_zconv(S, KXY, pitch, ny, ncols, kplanes, hz, scale, conj, az, cols_log2, threads, st);
 }
@@ -1470,7 +1485,12 @@ int fc_conv3d_device(const float* d_image, float* d_out, const int* imDim, const
   clear_status();
   return guarded([&] {
     if (!d_image || !d_out || !d_kernel) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
-    if (flags & (FC_FLAG_TC_FP16 | FC_FLAG_TC_BF16)) FC_THROW(FC_ERR_UNSUPPORTED, "tensor-core mode not built yet");
+    if ((flags & FC_FLAG_TC_FP16) && (flags & FC_FLAG_TC_BF16))
+      FC_THROW(FC_ERR_ARG, "choose one of FC_FLAG_TC_FP16 and FC_FLAG_TC_BF16");
+    struct TcScope {
+      explicit TcScope(int m) { t_tc_mode = m; }
+      ~TcScope() { t_tc_mode = 0; }
+    } tc_scope((flags & FC_FLAG_TC_FP16) ? 1 : (flags & FC_FLAG_TC_BF16) ? 2 : 0);
     int nx, ny, nz, kx = 0, ky = 0, kz = 0;
     dims3(imDim, &nx, &ny, &nz);
     const bool dense = flags & FC_FLAG_DENSE_KERNEL;

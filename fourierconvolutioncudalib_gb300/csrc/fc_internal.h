@@ -94,6 +94,24 @@ cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, in
 cudaError_t fast_zcorr(const float2* X, const float2* G, float2* out, long long pitch, int ny, int ncols, int kz,
                        int hz, float scale, const FcAxis& az, cudaStream_t st);
 
+// Tensor-core precision mode (fc_tc.cu, compiled for fp16 and for bf16):
+// register-resident kernels whose radix-16 stages run on the tensor cores,
+// lengths 128, 256, 512, 1024.  tc_cols mode: 0 forward, 1 inverse, 2 kernel
+// forward from the compact x-spectrum rows.  tc_x_r2c: taps != NULL selects
+// the kernel-tap source (kx, hx), else the dense rows `in`.
+#define FC_TC_DECL(sfx)                                                                                           \
+  cudaError_t tc_x_r2c##sfx(const float* in, long long in_pitch, const float* taps, int kx, int hx, float2* out,   \
+                            long long out_pitch, long long nrows, const FcAxis& ax, cudaStream_t st);               \
+  cudaError_t tc_x_c2r##sfx(const float2* in, long long in_pitch, float* out, long long out_pitch, long long nrows, \
+                            const FcAxis& ax, cudaStream_t st);                                                     \
+  cudaError_t tc_cols##sfx(int mode, const float2* src, long long src_pitch, int krows, int hy, float2* dst,        \
+                           long long ps, long long es, int ncols, int nplanes, const FcAxis& ax, cudaStream_t st);  \
+  cudaError_t tc_zconv##sfx(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,  \
+                            float scale, const FcAxis& az, cudaStream_t st);
+FC_TC_DECL(_fp16)
+FC_TC_DECL(_bf16)
+#undef FC_TC_DECL
+
 // W[k] = exp(-2 pi i k / n) computed on the device (double precision, rounded once)
 cudaError_t launch_make_twiddles(float2* W, int n, cudaStream_t st);
 
