@@ -82,6 +82,29 @@ struct Plan {
     return t;
   }
   static constexpr int T = max_a();
+  // Stage-twiddle tables, stored after the n roots W[0..n) of the axis table:
+  // for stage i >= 1 of a chain (NS = product of the earlier radices, radix R,
+  // TWS = N / (NS R)) a block of R-1 rows of NS entries, entry (r, k) =
+  // W[k r TWS] at (r-1)*NS + k (consecutive threads read consecutive k);
+  // forward chain first, then the reversed chain.  The entries are copies of
+  // W, so results do not depend on the layout.
+  __host__ __device__ static constexpr int ns(int i, bool rev) {
+    int p = 1;
+    for (int k = 0; k < i; ++k) p *= radix(k, rev);
+    return p;
+  }
+  __host__ __device__ static constexpr int tab_size(bool rev) {
+    int s = 0;
+    for (int i = 1; i < S; ++i) s += ns(i, rev) * (radix(i, rev) - 1);
+    return s;
+  }
+  __host__ __device__ static constexpr int tab_off(bool rev, int i) {
+    int o = N;
+    if (rev) o += tab_size(false);
+    for (int k = 1; k < i; ++k) o += ns(k, rev) * (radix(k, rev) - 1);
+    return o;
+  }
+  __host__ __device__ static constexpr int tab_total() { return N + tab_size(false) + tab_size(true); }
   __host__ __device__ static constexpr bool supported() {
     if (N < 2) return false;
     for (int i = 0; i < S; ++i)
@@ -94,9 +117,15 @@ struct Plan {
 
 __device__ __forceinline__ int rpad(int i) { return i + (i >> 4); }
 
-// shared-memory view of one row line
+// Shared-memory layouts of a line: position i lives at at(i) = base + i*E +
+// (D ? i / D : 0) (+ column offset), one pad word per D positions against bank
+// conflicts.  A run i0 + m*step (m = 0, 1, ...) is at at(i0) + run_off(m, step)
+// whenever no run crosses pad boundaries differently from its first element
+// (lin_write / lin_read below), so its addresses fold into constant offsets.
 struct RowLay {
   float2* base;
+  static constexpr int E = 1, D = 16;
+  __device__ __forceinline__ float2* at(int i) const { return base + rpad(i); }
   __device__ __forceinline__ float2& operator[](int i) const { return base[rpad(i)]; }
 };
 // column tile: B adjacent columns, position i of column c
@@ -104,27 +133,46 @@ template <int B>
 struct ColLay {
   float2* base;
   int c;
-  __device__ __forceinline__ float2& operator[](int i) const {
+  static constexpr int E = B >= 16 ? B + B / 16 : B;
+  static constexpr int D = B >= 16 ? 0 : 16 / B;
+  __device__ __forceinline__ float2* at(int i) const {
     const int q = i * B;
-    return base[q + c + (q >> 4)];
+    return base + q + c + (q >> 4);
   }
+  __device__ __forceinline__ float2& operator[](int i) const { return *at(i); }
 };
 
-template <int N, int R, int NS, bool INV, int TCM>
+template <class L>
+__host__ __device__ constexpr int run_off(int m, int step) {
+  return m * step * L::E + (L::D ? (m * step) / L::D : 0);
+}
+// Stockham write run: base = (j - k) R + k with k = j mod NS < NS, elements
+// base + m NS (m < R) inside the NS*R-aligned block of the butterfly
+template <class L>
+__host__ __device__ constexpr bool lin_write(int NS, int R) {
+  return L::D == 0 || NS % L::D == 0 || (L::D % NS == 0 && ((NS * R) % L::D == 0 || L::D % (NS * R) == 0));
+}
+// read run: j + m NB (any j)
+template <class L>
+__host__ __device__ constexpr bool lin_read(int NB) {
+  return L::D == 0 || NB % L::D == 0;
+}
+
+template <int N, int I, int R, int NS, bool INV, int TCM>
 __device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const float2* __restrict__ W,
                                       const TcCtx& tcx) {
   constexpr int U = kVals / R;
   constexpr int A = Plan<N>::A(R);
   constexpr int NB = N / R;
-  constexpr int TWS = N / (NS * R);
-  // butterflies a thread does not own compute on stale registers and are never stored;
-  // their twiddle index stays below N
+  // butterflies a thread does not own compute on stale registers and are never
+  // stored; their twiddle row k = (t + b*A) mod NS stays inside the table
 #pragma unroll
   for (int b = 0; b < U; ++b) {
     if (NS > 1) {
       const int k = (t + b * A) % NS;
+      const float2* tw = W + Plan<N>::tab_off(INV, I) + k;
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[b * R + r] = c_tw<INV>(v[b * R + r], __ldg(W + k * r * TWS));
+      for (int r = 1; r < R; ++r) v[b * R + r] = c_tw<INV>(v[b * R + r], __ldg(tw + (r - 1) * NS));
     }
     if constexpr (TCM != tc::kNone && R == 16)
       tc::dft16<INV, TCM>(&v[b * R], tcx.ws, tcx.tab);
@@ -145,8 +193,14 @@ __device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const 
     if (j < NB && t < A) {
       const int k = j % NS;
       const int base = (j - k) * R + k;
+      if constexpr (lin_write<L>(NS, R)) {
+        float2* p = sm.at(base);
 #pragma unroll
-      for (int m = 0; m < R; ++m) sm[base + m * NS] = v[b * R + m];
+        for (int m = 0; m < R; ++m) p[run_off<L>(m, NS)] = v[b * R + m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < R; ++m) sm[base + m * NS] = v[b * R + m];
+      }
     }
   }
   __syncthreads();
@@ -154,8 +208,14 @@ __device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const 
   for (int b = 0; b < U2; ++b) {
     const int j = t + b * A2;
     if (j < NB2 && t < A2) {
+      if constexpr (lin_read<L>(NB2)) {
+        const float2* p = sm.at(j);
 #pragma unroll
-      for (int m = 0; m < R2; ++m) v[b * R2 + m] = sm[j + m * NB2];
+        for (int m = 0; m < R2; ++m) v[b * R2 + m] = p[run_off<L>(m, NB2)];
+      } else {
+#pragma unroll
+        for (int m = 0; m < R2; ++m) v[b * R2 + m] = sm[j + m * NB2];
+      }
     }
   }
   __syncthreads();
@@ -168,7 +228,7 @@ struct Chain {
   static __device__ __forceinline__ void run(float2 (&v)[kVals], const L& sm, const int t,
                                              const float2* __restrict__ W, const TcCtx& tcx) {
     constexpr int R = Plan<N>::radix(I, INV);
-    stage<N, R, NS, INV, TCM>(v, t, W, tcx);
+    stage<N, I, R, NS, INV, TCM>(v, t, W, tcx);
     if constexpr (I + 1 < Plan<N>::S) {
       constexpr int R2 = Plan<N>::radix(I + 1, INV);
       exchange<N, R, NS, R2>(v, sm, t);

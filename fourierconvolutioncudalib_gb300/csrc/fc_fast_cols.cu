@@ -28,7 +28,55 @@ static cudaError_t dispatch_cols(int n, Src src, float2* dst, long long ps, long
   }
 }
 
+// Fill the stage-twiddle tables of length N (layout: Plan<N>::tab_off) from
+// the roots W[0..N) already in the table.
+template <int N>
+__global__ void k_stage_twiddles(float2* __restrict__ W) {
+  constexpr ChainC C = Plan<N>::C;
+  const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x), nth = (int)(gridDim.x * blockDim.x);
+  for (int rev = 0; rev < 2; ++rev) {
+    int ns = 1;
+    int off = rev ? Plan<N>::tab_off(true, 1) : Plan<N>::tab_off(false, 1);
+    for (int i = 0; i < Plan<N>::S; ++i) {
+      const int R = C.r[rev ? Plan<N>::S - 1 - i : i];
+      if (i >= 1) {
+        for (int e = tid; e < ns * (R - 1); e += nth) {
+          const int r = 1 + e / ns, k = e - (r - 1) * ns;
+          W[off + e] = W[k * r * (N / (ns * R))];  // k*r*TWS < N
+        }
+        off += ns * (R - 1);
+      }
+      ns *= R;
+    }
+  }
+}
+
 }  // namespace fast
+
+long long fast_twiddle_count(int n) {
+  switch (n) {
+#define FC_CASE(n_) \
+  case n_:          \
+    return fast::Plan<n_>::tab_total();
+    FC_ROW_SIZES(FC_CASE)
+#undef FC_CASE
+    default:
+      return n;
+  }
+}
+
+cudaError_t launch_stage_twiddles(float2* W, int n, cudaStream_t st) {
+  switch (n) {
+#define FC_CASE(n_)                                     \
+  case n_:                                              \
+    fast::k_stage_twiddles<n_><<<8, 256, 0, st>>>(W); \
+    return cudaGetLastError();
+    FC_ROW_SIZES(FC_CASE)
+#undef FC_CASE
+    default:
+      return cudaSuccess;
+  }
+}
 
 bool fast_cols_supported(int n) {
   switch (n) {

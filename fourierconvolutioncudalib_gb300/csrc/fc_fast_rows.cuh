@@ -25,69 +25,100 @@ struct RowGeom {
   static constexpr int THREADS = LPB * T;
   static constexpr int LS = N + N / 16 + 2;  // padded line stride
   static constexpr int SMEM = LPB * LS;       // float2 elements
-  static long long tiles(long long nrows) { return (nrows + 2LL * LPB - 1) / (2LL * LPB); }
+  __host__ __device__ static long long tiles(long long nrows) { return (nrows + 2LL * LPB - 1) / (2LL * LPB); }
 };
+
+// line / thread split of a row tile: tile rows ra = 2*(tile*LPB + line), rb = ra + 1
+template <int N>
+struct RowSlot {
+  bool act, va, vb;
+  int line, t;
+  long long ra, rb;
+  __device__ __forceinline__ RowSlot(long long tile, int tid, long long nrows) {
+    using G = RowGeom<N>;
+    act = tid < G::THREADS;
+    line = act ? tid / G::T : 0;
+    t = act ? tid - line * G::T : G::T;  // inert threads own no butterfly
+    ra = (tile * G::LPB + line) * 2;
+    rb = ra + 1;
+    va = act && ra < nrows;
+    vb = act && rb < nrows;
+  }
+};
+
+// first-stage values of the R2C: z = a + i b for real rows a, b of the slot
+template <int N, class Src>
+__device__ __forceinline__ void load_r2c(float2 (&v)[kVals], const Src& src, const RowSlot<N>& s) {
+  constexpr int R0 = first_radix<N, false>();
+#pragma unroll
+  for (int q = 0; q < kVals; ++q) {
+    const int x = stage_pos<N, R0>(s.t, q);
+    v[q] = make_float2(0.f, 0.f);
+    if (x >= 0) v[q] = make_float2(s.va ? src.load(s.ra, x) : 0.f, s.vb ? src.load(s.rb, x) : 0.f);
+  }
+}
+
+// transform of the loaded values, separation of the two half spectra, stores
+template <int N, int TCM = tc::kNone>
+__device__ __forceinline__ void finish_r2c(float2 (&v)[kVals], const RowSlot<N>& s, float2* __restrict__ out,
+                                           long long out_pitch, const float2* __restrict__ W, float2* sm,
+                                           const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+  using G = RowGeom<N>;
+  constexpr int RF = last_radix<N, false>();
+  constexpr int NBF = N / RF, UF = kVals / RF, AF = Plan<N>::A(RF);
+  float2* lbase = sm + s.line * G::LS;
+  const RowLay lay{lbase};
+  fft<N, false, TCM>(v, lay, s.t, W, tcx);
+  // natural-order outputs x = j + m*NBF of the last stage into the line
+#pragma unroll
+  for (int b = 0; b < UF; ++b) {
+    const int j = s.t + b * AF;
+    if (j < NBF && s.t < AF) {
+      if constexpr (lin_read<RowLay>(NBF)) {
+        float2* p = lay.at(j);
+#pragma unroll
+        for (int m = 0; m < RF; ++m) p[run_off<RowLay>(m, NBF)] = v[b * RF + m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < RF; ++m) lay[j + m * NBF] = v[b * RF + m];
+      }
+    }
+  }
+  __syncthreads();
+  if (s.act) {
+    for (int k = s.t; k <= N / 2; k += G::T) {
+      const float2 zk = lbase[rpad(k)];
+      const float2 zn = lbase[rpad(k == 0 ? 0 : N - k)];
+      if (s.va) out[s.ra * out_pitch + k] = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+      if (s.vb) out[s.rb * out_pitch + k] = make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x));
+    }
+  }
+}
 
 template <int N, class Src, int TCM = tc::kNone>
 __device__ __forceinline__ void body_r2c(const Src& src, float2* __restrict__ out, long long out_pitch,
                                          long long nrows, const float2* __restrict__ W, long long tile, int tid,
                                          float2* sm, const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
-  using G = RowGeom<N>;
-  constexpr int R0 = first_radix<N, false>();
-  constexpr int RF = last_radix<N, false>();
-  const bool act = tid < G::THREADS;
-  const int line = act ? tid / G::T : 0;
-  const int t = act ? tid - line * G::T : G::T;  // inert threads own no butterfly
-  const long long ra = (tile * G::LPB + line) * 2, rb = ra + 1;
-  const bool va = act && ra < nrows, vb = act && rb < nrows;
-  float2* lbase = sm + line * G::LS;
+  const RowSlot<N> s(tile, tid, nrows);
   float2 v[kVals];
-#pragma unroll
-  for (int q = 0; q < kVals; ++q) {
-    const int x = stage_pos<N, R0>(t, q);
-    v[q] = make_float2(0.f, 0.f);
-    if (x >= 0) v[q] = make_float2(va ? src.load(ra, x) : 0.f, vb ? src.load(rb, x) : 0.f);
-  }
-  fft<N, false, TCM>(v, RowLay{lbase}, t, W, tcx);
-#pragma unroll
-  for (int q = 0; q < kVals; ++q) {
-    const int x = stage_pos<N, RF>(t, q);
-    if (x >= 0) lbase[rpad(x)] = v[q];
-  }
-  __syncthreads();
-  if (act) {
-    for (int k = t; k <= N / 2; k += G::T) {
-      const float2 zk = lbase[rpad(k)];
-      const float2 zn = lbase[rpad(k == 0 ? 0 : N - k)];
-      if (va) out[ra * out_pitch + k] = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
-      if (vb) out[rb * out_pitch + k] = make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x));
-    }
-  }
+  load_r2c<N>(v, src, s);
+  finish_r2c<N, TCM>(v, s, out, out_pitch, W, sm, tcx);
 }
 
-template <int N, int TCM = tc::kNone>
-__device__ __forceinline__ void body_c2r(const float2* __restrict__ in, long long in_pitch, float* __restrict__ out,
-                                         long long out_pitch, long long nrows, const float2* __restrict__ W,
-                                         long long tile, int tid, float2* sm,
-                                         const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
-  using G = RowGeom<N>;
+// first-stage values of the C2R: the Hermitian extension of two half-spectrum
+// rows a, b (read through `in` with row pitch in_pitch), packed as A + i B
+template <int N, class In>
+__device__ __forceinline__ void load_c2r(float2 (&v)[kVals], const In& in, const RowSlot<N>& s) {
   constexpr int R0 = first_radix<N, true>();
-  constexpr int RF = last_radix<N, true>();
-  const bool act = tid < G::THREADS;
-  const int line = act ? tid / G::T : 0;
-  const int t = act ? tid - line * G::T : G::T;
-  const long long ra = (tile * G::LPB + line) * 2, rb = ra + 1;
-  const bool va = act && ra < nrows, vb = act && rb < nrows;
-  float2 v[kVals];
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
-    const int k = stage_pos<N, R0>(t, q);
+    const int k = stage_pos<N, R0>(s.t, q);
     v[q] = make_float2(0.f, 0.f);
     if (k >= 0) {
       const bool lo = k <= N / 2;
       const int kk = lo ? k : N - k;
-      float2 a = va ? in[ra * in_pitch + kk] : make_float2(0.f, 0.f);
-      float2 b = vb ? in[rb * in_pitch + kk] : make_float2(0.f, 0.f);
+      float2 a = s.va ? in.load(s.ra, kk) : make_float2(0.f, 0.f);
+      float2 b = s.vb ? in.load(s.rb, kk) : make_float2(0.f, 0.f);
       if (kk == 0 || 2 * kk == N) {
         a.y = 0.f;
         b.y = 0.f;
@@ -99,15 +130,41 @@ __device__ __forceinline__ void body_c2r(const float2* __restrict__ in, long lon
       v[q] = make_float2(a.x - b.y, a.y + b.x);
     }
   }
-  fft<N, true, TCM>(v, RowLay{sm + line * G::LS}, t, W, tcx);
+}
+
+template <int N, int TCM = tc::kNone>
+__device__ __forceinline__ void finish_c2r(float2 (&v)[kVals], const RowSlot<N>& s, float* __restrict__ out,
+                                           long long out_pitch, const float2* __restrict__ W, float2* sm,
+                                           const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+  using G = RowGeom<N>;
+  constexpr int RF = last_radix<N, true>();
+  fft<N, true, TCM>(v, RowLay{sm + s.line * G::LS}, s.t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
-    const int x = stage_pos<N, RF>(t, q);
+    const int x = stage_pos<N, RF>(s.t, q);
     if (x >= 0) {
-      if (va) out[ra * out_pitch + x] = v[q].x;
-      if (vb) out[rb * out_pitch + x] = v[q].y;
+      if (s.va) out[s.ra * out_pitch + x] = v[q].x;
+      if (s.vb) out[s.rb * out_pitch + x] = v[q].y;
     }
   }
+}
+
+// complex half-spectrum rows in global memory
+struct HalfRows {
+  const float2* p;
+  long long pitch;
+  __device__ __forceinline__ float2 load(long long row, int k) const { return p[row * pitch + k]; }
+};
+
+template <int N, int TCM = tc::kNone>
+__device__ __forceinline__ void body_c2r(const float2* __restrict__ in, long long in_pitch, float* __restrict__ out,
+                                         long long out_pitch, long long nrows, const float2* __restrict__ W,
+                                         long long tile, int tid, float2* sm,
+                                         const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+  const RowSlot<N> s(tile, tid, nrows);
+  float2 v[kVals];
+  load_c2r<N>(v, HalfRows{in, in_pitch}, s);
+  finish_c2r<N, TCM>(v, s, out, out_pitch, W, sm, tcx);
 }
 
 }  // namespace fast

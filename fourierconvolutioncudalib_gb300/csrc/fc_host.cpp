@@ -180,8 +180,10 @@ static const float2* twiddles_for(DevCtx& c, int n) {
     h[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
   }
   float2* d = nullptr;
-  cuda_check(cudaMalloc(&d, sizeof(float2) * n), "cudaMalloc(twiddles)");
+  cuda_check(cudaMalloc(&d, sizeof(float2) * (size_t)fast_twiddle_count(n)), "cudaMalloc(twiddles)");
   cuda_check(cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice), "cudaMemcpy(twiddles)");
+  cuda_check(launch_stage_twiddles(d, n, nullptr), "stage twiddles");
+  cuda_check(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize(twiddles)");
   c.twiddles[n] = d;
   return d;
 }
@@ -290,7 +292,14 @@ struct ProfRec {
 };
 static std::mutex g_prof_mu;
 static bool g_prof_on = false;
+static std::string g_prof_only;  // record only the pass of this name (empty: all)
 static std::vector<ProfRec> g_prof;
+
+static bool prof_wants(const char* name) {
+  if (!g_prof_on || t_no_events) return false;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  return g_prof_only.empty() || g_prof_only == name;
+}
 
 struct PassScope {
   bool on;
@@ -298,7 +307,7 @@ struct PassScope {
   const char* name;
   double bytes;
   cudaStream_t st;
-  PassScope(const char* nm, double by, cudaStream_t s) : on(g_prof_on && !t_no_events), name(nm), bytes(by), st(s) {
+  PassScope(const char* nm, double by, cudaStream_t s) : on(prof_wants(nm)), name(nm), bytes(by), st(s) {
     if (on) {
       cudaEventCreate(&a);
       cudaEventCreate(&b);
@@ -339,10 +348,31 @@ static thread_local int t_tc_mode = 0;
 static bool tc_len(int n) { return n == 128 || n == 256 || n == 512 || n == 1024; }
 #define FC_TC_CALL(fn, ...) (t_tc_mode == 1 ? fn##_fp16(__VA_ARGS__) : fn##_bf16(__VA_ARGS__))
 
+// Pipelined x passes (fc_fast_pipe.cu); FC_PIPE=0 selects the one-tile-per-CTA kernels.
+static int g_pipe = -1;
+static bool use_pipe() {
+  if (g_pipe < 0) {
+    const char* e = std::getenv("FC_PIPE");
+    g_pipe = e ? std::atoi(e) : 1;
+  }
+  return g_pipe != 0;
+}
+// set while the enqueue in progress on this thread reads the image from host memory
+static thread_local bool t_host_src = false;
+struct HostSrcScope {
+  bool prev;
+  explicit HostSrcScope(bool on) : prev(t_host_src) { t_host_src = on; }
+  ~HostSrcScope() { t_host_src = prev; }
+};
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
 static cudaError_t d_x_r2c_dense(const float* in, long long ip, float2* out, long long op, long long rows,
                                  const FcAxis& ax, const Tiles& t, cudaStream_t st) {
   if (t_tc_mode && tc_len(ax.n)) return FC_TC_CALL(tc_x_r2c, in, ip, nullptr, 0, 0, out, op, rows, ax, st);
-  if (use_fast() && fast_rows_supported(ax.n)) return fast_x_r2c_dense(in, ip, out, op, rows, ax, st);
+  if (use_fast() && fast_rows_supported(ax.n)) {
+    if (use_pipe() && !t_host_src && aligned16(in) && ip % 4 == 0) return pipe_x_r2c_dense(in, ip, out, op, rows, ax, st);
+    return fast_x_r2c_dense(in, ip, out, op, rows, ax, st);
+  }
   return launch_x_r2c_dense(in, ip, out, op, rows, ax, t, st);
 }
 static cudaError_t d_x_r2c_box(const float* taps, int kx, int hx, float2* out, long long op, long long rows,
@@ -354,7 +384,10 @@ static cudaError_t d_x_r2c_box(const float* taps, int kx, int hx, float2* out, l
 static cudaError_t d_x_c2r(const float2* in, long long ip, float* out, long long op, long long rows, const FcAxis& ax,
                            const Tiles& t, cudaStream_t st) {
   if (t_tc_mode && tc_len(ax.n)) return FC_TC_CALL(tc_x_c2r, in, ip, out, op, rows, ax, st);
-  if (use_fast() && fast_rows_supported(ax.n)) return fast_x_c2r(in, ip, out, op, rows, ax, st);
+  if (use_fast() && fast_rows_supported(ax.n)) {
+    if (use_pipe() && aligned16(in) && ip % 2 == 0) return pipe_x_c2r(in, ip, out, op, rows, ax, st);
+    return fast_x_c2r(in, ip, out, op, rows, ax, st);
+  }
   return launch_x_c2r(in, ip, out, op, rows, ax, t, st);
 }
 static cudaError_t d_cols(const float2* src, float2* dst, long long ps, long long es, int ncols, int nplanes, bool inv,
@@ -524,10 +557,10 @@ static void enqueue_conv_core(const Geom& g0, const Axes& a, const float* d_imag
   float2* S = (float2*)(ws + L.off_S);
   const long long rows = (long long)g.ny * g.nz;
   const long long ps = (long long)g.ny * g.pitch;
+  const int cw = chunk_cols(g);
   enqueue_kernel_x(g, a, t, ksrc, ws, L, st);
   FC_PASS("image_x_r2c", 4.0 * g.N() + 8.0 * g.nxh * rows, st,
           d_x_r2c_dense(d_image, g.nx, S, g.pitch, rows, a.x, t, st));
-  const int cw = chunk_cols(g);
   for (int c0 = 0; c0 < g.nxh; c0 += cw) {
     const int w = std::min(cw, g.nxh - c0);
     enqueue_kernel_y(g, a, t, ws, L, c0, w, st);
@@ -539,7 +572,8 @@ static void enqueue_conv_core(const Geom& g0, const Axes& a, const float* d_imag
     FC_PASS("image_y_inv", 16.0 * w * (double)rows, st,
             d_cols(S + c0, S + c0, ps, g.pitch, w, g.nz, true, a.y, t.y_cols_log2, t.threads, st));
   }
-  FC_PASS("image_x_c2r", 4.0 * g.N() + 8.0 * g.nxh * rows, st, d_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
+  FC_PASS("image_x_c2r", 4.0 * g.N() + 8.0 * g.nxh * rows, st,
+          d_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
 }
 
 // ------------------------------------------------------------------ adjoint
@@ -713,8 +747,12 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
   cuda_check(cudaMemcpyAsync(c.d_ker, kernel, nker, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(kernel H2D)");
   const int mode = host_io_mode();
   if (allow_direct && mode != 0 && device_reads_pageable(dev) && (mode == 1 || host_buffer_pinned(im))) {
-    enqueue_conv(c, g, im, out, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
+    {
+      HostSrcScope hs(true);
+      enqueue_conv(c, g, im, out, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
+    }
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (pipe_take_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in a pipelined pass");
     return;
   }
   grow((void**)&c.d_img, &c.img_cap, nimg, "cudaMalloc(image)");
@@ -722,6 +760,7 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
   enqueue_conv(c, g, c.d_img, c.d_img, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
   cuda_check(cudaMemcpyAsync(out, c.d_img, nimg, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync(result D2H)");
   cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  if (pipe_take_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in a pipelined pass");
 }
 
 template <class F>
@@ -1244,7 +1283,8 @@ int conv_in_scratch(const float* d_image, float* d_out, const int* imDim, const 
     if (!dense) dims3(kernelDim, &kx, &ky, &kz);
     const Geom g = make_geom(nx, ny, nz, kx, ky, kz, dense);
     const bool compat = (flags & FC_FLAG_SHIFT_COMPAT) && g.kbox;
-    const size_t tw = align256(sizeof(float2) * ((size_t)nx + ny + nz));
+    const size_t tw =
+        align256(sizeof(float2) * (size_t)(fast_twiddle_count(nx) + fast_twiddle_count(ny) + fast_twiddle_count(nz)));
     const size_t need = tw + plain_layout(g, compat).total;
     if (need > scratch_bytes)
       FC_THROW(FC_ERR_NOMEM, "this convolution needs " + std::to_string(need) + " bytes of scratch; the static scratch "
@@ -1265,8 +1305,9 @@ int conv_in_scratch(const float* d_image, float* d_out, const int* imDim, const 
       for (int k = 0; k < ns; ++k) ax.radix[k] = r[k];
       ax.W = W + off;
       cuda_check(launch_make_twiddles(W + off, n3[i], st), "twiddles");
-      ++t_launches;
-      off += (size_t)n3[i];
+      cuda_check(launch_stage_twiddles(W + off, n3[i], st), "stage twiddles");
+      t_launches += 2;
+      off += (size_t)fast_twiddle_count(n3[i]);
     }
     struct NoEvents {
       NoEvents() { t_no_events = true; }
@@ -1641,6 +1682,11 @@ int fc_conv3d_batched_device(int n_views, const float* const* d_images, float* c
 void fc_profile_enable(int on) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   g_prof_on = on != 0;
+}
+
+void fc_profile_only(const char* pass_name) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_only = pass_name ? pass_name : "";
 }
 
 int fc_profile_read(char* names, int name_stride, float* ms, double* bytes, int max) {

@@ -87,6 +87,22 @@ cudaError_t fast_x_c2r(const float2* in, long long in_pitch, float* out, long lo
                        const FcAxis& ax, cudaStream_t st);
 cudaError_t fast_cols(const float2* src, float2* dst, long long ps, long long es, int ncols, int nplanes, bool inverse,
                       const FcAxis& ax, cudaStream_t st);
+// Axis twiddle tables: W[0..n) followed, for lengths of the register-resident
+// kernels, by their stage-twiddle tables (fc_fast.cuh, Plan<N>::tab_off).
+// fast_twiddle_count(n) is the table length in float2 entries (n for other
+// lengths); launch_stage_twiddles fills the stage part from W[0..n).
+long long fast_twiddle_count(int n);
+cudaError_t launch_stage_twiddles(float2* W, int n, cudaStream_t st);
+
+// Pipelined x passes (fc_fast_pipe.cu): persistent CTAs with bulk
+// asynchronous tile copies.  in must be device memory, 16-byte aligned, with
+// rows of a multiple of 16 bytes.  pipe_take_timeouts() returns and clears the
+// number of bounded waits that expired.
+cudaError_t pipe_x_r2c_dense(const float* in, long long in_pitch, float2* out, long long out_pitch, long long nrows,
+                             const FcAxis& ax, cudaStream_t st);
+cudaError_t pipe_x_c2r(const float2* in, long long in_pitch, float* out, long long out_pitch, long long nrows,
+                       const FcAxis& ax, cudaStream_t st);
+unsigned int pipe_take_timeouts();
 cudaError_t fast_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
                          int nplanes, const FcAxis& ax, cudaStream_t st);
 cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,

@@ -159,11 +159,13 @@ def pad_shift_kernel(kernel: torch.Tensor, image_shape: Sequence[int], flags: in
     return out
 
 
-def profile(enable: Optional[bool] = None) -> List[Tuple[str, float, float]]:
-    """Enable/disable per-pass event timing; with no argument, read and clear
-    the records: list of (pass name, milliseconds, algorithmic bytes)."""
+def profile(enable: Optional[bool] = None, only: Optional[str] = None) -> List[Tuple[str, float, float]]:
+    """Enable/disable per-pass event timing (``only``: record just the pass of
+    that name); with no argument, read and clear the records: list of
+    (pass name, milliseconds, algorithmic bytes)."""
     L = lib()
     if enable is not None:
+        L.fc_profile_only((only or "").encode())
         L.fc_profile_enable(1 if enable else 0)
         return []
     cap = 4096

@@ -177,6 +177,8 @@ FUNCTION_PREFIX int fc_plan_radices(int n, int* radices, int max_stages);
  * entries (name, milliseconds, algorithmic bytes) of the most recent call(s),
  * then clears the record. */
 FUNCTION_PREFIX void fc_profile_enable(int on);
+/* restrict the per-pass events to the pass of this name (NULL or "": all) */
+FUNCTION_PREFIX void fc_profile_only(const char* pass_name);
 FUNCTION_PREFIX int fc_profile_read(char* names, int name_stride, float* ms, double* bytes, int max);
 /* number of kernel launches the most recent fc_* / reference call made */
 FUNCTION_PREFIX int fc_launch_count(void);
