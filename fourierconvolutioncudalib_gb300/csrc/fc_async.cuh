@@ -64,5 +64,14 @@ __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
   return true;
 }
 
+// per-thread 16-byte asynchronous copy global -> shared (cp.async, L1 bypass);
+// both addresses 16-byte aligned.  Completion: commit(), then wait_all() in the
+// issuing thread, then a CTA barrier before other threads read the data.
+__device__ __forceinline__ void copy16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 }  // namespace async
 }  // namespace fc

@@ -12,6 +12,7 @@
 #ifndef FC_ZCONV_MIN_BLOCKS
 #define FC_ZCONV_MIN_BLOCKS 2
 #endif
+#include "fc_async.cuh"
 #include "fc_fast.cuh"
 #include "fc_fast_sizes.h"
 #include "fc_internal.h"
@@ -20,17 +21,19 @@
 namespace fc {
 namespace fast {
 
-template <int N>
-struct ColGeom {
+// columns per tile: the largest power of two <= BMAX with N*B <= 4096 values
+// and B*T <= 256 threads (4 at least)
+template <int N, int BMAX = 32>
+struct ColGeomB {
   static constexpr int T = Plan<N>::T;
-  // columns per tile: the largest power of two <= 32 with N*B <= 4096 values
-  // and B*T <= 256 threads (4 at least)
   static constexpr int B0a = 4096 / N, B0b = 256 / T;
-  static constexpr int B0 = B0a < B0b ? B0a : B0b;
+  static constexpr int B0 = (B0a < B0b ? B0a : B0b) < BMAX ? (B0a < B0b ? B0a : B0b) : BMAX;
   static constexpr int B = B0 >= 32 ? 32 : B0 >= 16 ? 16 : B0 >= 8 ? 8 : 4;
   static constexpr int THREADS = B * T;
   static constexpr int SMEM = N * B + (N * B) / 16;  // float2 elements of the exchange tile
 };
+template <int N>
+using ColGeom = ColGeomB<N, 32>;
 
 // y pass body: tile (bx, plane) = columns [bx*B, bx*B + B) of one plane.
 template <int N, bool INV, class Src, int TCM = tc::kNone>
@@ -70,46 +73,78 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* d
 
 // Fused z pass.  Kernel plane p of KXY holds z = (p - hz) mod nz.  The
 // kernel column is transformed first and parked in a per-thread private
-// shared-memory stash (stash[q*THREADS + tid], no barrier needed), so only
-// one column's values are live in registers during the image transform.
+// shared-memory stash (stash[q*nstash + tid], no barrier needed), so only one
+// column's values are live in registers during the image transform.  With a
+// stage buffer, the image tile (N rows of B columns) is copied into shared
+// memory asynchronously at the start, while the kernel column is loaded and
+// transformed.
+//
+// The single-volume kernel uses tiles of at most 16 columns: the spectrum has
+// nx/2+1 columns, and narrower tiles waste less work on the ragged last tile.
+template <int N>
+using ZTile = ColGeomB<N, 16>;
 template <int N>
 struct ZGeom {
-  static constexpr int SMEM_BYTES = (ColGeom<N>::SMEM + ColGeom<N>::THREADS * kVals) * (int)sizeof(float2);
+  // exchange tile, stash, image stage buffer (float2 elements)
+  static constexpr int STAGE = N * ZTile<N>::B;
+  static constexpr int SMEM_BYTES =
+      (ZTile<N>::SMEM + ZTile<N>::THREADS * kVals + STAGE) * (int)sizeof(float2);
   // resident CTAs requested from the register allocator (256 threads: 2 -> <= 128 registers)
-  static constexpr int MIN_BLOCKS = ColGeom<N>::THREADS <= 256 ? FC_ZCONV_MIN_BLOCKS : 1;
+  static constexpr int MIN_BLOCKS =
+      ZTile<N>::THREADS <= 256 ? FC_ZCONV_MIN_BLOCKS * (256 / ZTile<N>::THREADS) : 1;
 };
 
-// fused z pass body: tile (bx, ky); stash holds nstash >= THREADS slots per value index
-template <int N, bool CONJ, int TCM = tc::kNone>
+// fused z pass body: tile (bx, ky); stash holds nstash >= THREADS slots per value index;
+// stage (optional) holds N*B float2 for the prefetched image tile
+template <int N, bool CONJ, int TCM = tc::kNone, class G = ColGeom<N>>
 __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch,
                                            int ny, int ncols, int kplanes, int hz, float scale,
                                            const float2* __restrict__ W, int bx, int ky, int tid, float2* sm,
-                                           float2* stash, int nstash, const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
-  using G = ColGeom<N>;
+                                           float2* stash, int nstash, const TcCtx& tcx = TcCtx{nullptr, nullptr},
+                                           float2* stage = nullptr) {
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, false>(), RF = last_radix<N, true>();
   const int c = tid % B;
   const int t = tid / B;
-  const int col = bx * B + c;
+  const int col0 = bx * B;
+  const int col = col0 + c;
   const bool ok = col < ncols && t < G::T;
   const long long zs = (long long)ny * pitch;
   float2* base = S + (long long)ky * pitch + col;
+  if (stage) {
+    // 16-byte pieces (two columns) of the N x B image tile; pieces starting at
+    // or beyond ncols are skipped (the row pitch covers the second column)
+    const float2* src0 = S + (long long)ky * pitch + col0;
+    for (int e = tid; e < N * (B / 2); e += G::THREADS) {
+      const int z = e / (B / 2), part = e - z * (B / 2);
+      if (col0 + 2 * part < ncols) async::copy16(stage + z * B + 2 * part, src0 + z * zs + 2 * part);
+    }
+    async::commit();
+  }
   const ColLay<B> lay{sm, c};
   float2 v[kVals];
+  const float2* kbase = KXY + (long long)ky * pitch + col;
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int z = stage_pos<N, R0>(t, q);
     int p = z + hz;
     if (p >= N) p -= N;
-    v[q] = (ok && z >= 0 && p < kplanes) ? KXY[((long long)p * ny + ky) * pitch + col] : make_float2(0.f, 0.f);
+    v[q] = (ok && z >= 0 && p < kplanes) ? kbase[p * zs] : make_float2(0.f, 0.f);
   }
   fft<N, false, TCM>(v, lay, t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) stash[q * nstash + tid] = v[q];
+  if (stage) {
+    async::wait_all();
+    __syncthreads();
+  }
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int z = stage_pos<N, R0>(t, q);
-    v[q] = (ok && z >= 0) ? base[z * zs] : make_float2(0.f, 0.f);
+    if (stage)
+      v[q] = (ok && z >= 0) ? stage[z * B + c] : make_float2(0.f, 0.f);
+    else
+      v[q] = (ok && z >= 0) ? base[z * zs] : make_float2(0.f, 0.f);
   }
   fft<N, false, TCM>(v, lay, t, W, tcx);
   // the forward outputs sit where the inverse's first stage reads them
@@ -131,13 +166,22 @@ __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2*
 }
 
 template <int N, bool CONJ>
-__global__ void __launch_bounds__(ColGeom<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zconv(
+__global__ void __launch_bounds__(ZTile<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zconv(
     float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
     float scale, const float2* __restrict__ W) {
-  extern __shared__ float2 zsm[];
-  body_zconv<N, CONJ>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, W, (int)blockIdx.x, (int)blockIdx.y,
-                      (int)threadIdx.x, zsm, zsm + ColGeom<N>::SMEM, ColGeom<N>::THREADS);
+  using G = ZTile<N>;
+  extern __shared__ __align__(16) float2 zsm[];
+  float2* stash = zsm + G::SMEM;
+  float2* stage = stash + G::THREADS * kVals;
+  body_zconv<N, CONJ, tc::kNone, G>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, W, (int)blockIdx.x,
+                                    (int)blockIdx.y, (int)threadIdx.x, zsm, stash, G::THREADS,
+                                    TcCtx{nullptr, nullptr}, stage);
 }
+
+template <int N>
+struct CorrGeom {  // k_zcorr: exchange tile and stash of the 32-column geometry
+  static constexpr int SMEM_BYTES = (ColGeom<N>::SMEM + ColGeom<N>::THREADS * kVals) * (int)sizeof(float2);
+};
 
 // Kernel-gradient z pass: conj(X) * G * scale, inverse, keep kernel planes
 // p < kz where z = (p - hz) mod nz, written to out plane p.

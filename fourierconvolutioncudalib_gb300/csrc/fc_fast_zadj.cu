@@ -19,7 +19,7 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
   switch (az.n) {
 #define FC_CASE(n_)                                                                                             \
   case n_: {                                                                                                    \
-    using G = ColGeom<n_>;                                                                                      \
+    using G = ZTile<n_>;                                                                                        \
     constexpr int sm = ZGeom<n_>::SMEM_BYTES;                                                                   \
     dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                   \
     const cudaError_t e = set_dyn_smem(k_zconv<n_, CONJ>, sm);                                                  \
@@ -47,7 +47,7 @@ cudaError_t fast_zcorr(const float2* X, const float2* G_, float2* out, long long
 #define FC_CASE(n_)                                                                                          \
   case n_: {                                                                                                 \
     using G = fast::ColGeom<n_>;                                                                             \
-    constexpr int sm = fast::ZGeom<n_>::SMEM_BYTES;                                                          \
+    constexpr int sm = fast::CorrGeom<n_>::SMEM_BYTES;                                                          \
     dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                \
     const cudaError_t e = fast::set_dyn_smem(fast::k_zcorr<n_>, sm);                                         \
     if (e != cudaSuccess) return e;                                                                          \

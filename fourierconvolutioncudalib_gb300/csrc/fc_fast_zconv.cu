@@ -19,7 +19,7 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
   switch (az.n) {
 #define FC_CASE(n_)                                                                                             \
   case n_: {                                                                                                    \
-    using G = ColGeom<n_>;                                                                                      \
+    using G = ZTile<n_>;                                                                                        \
     constexpr int sm = ZGeom<n_>::SMEM_BYTES;                                                                   \
     dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                   \
     const cudaError_t e = set_dyn_smem(k_zconv<n_, CONJ>, sm);                                                  \
