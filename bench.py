@@ -545,6 +545,49 @@ def time_forms(dev, fcd, torch):
     tc["how"] = ("radix-16 stages as 32x32 real DFT products, mma.sync m16n8k16, per-column power-of-two scaling, "
                  "hi+lo 16-bit operands, fp32 accumulation")
     out["tensor_core"] = tc
+    # kernel-spectrum reuse: the image passes only, against the plain call (512x512x128, 31x31x63)
+    ks = fcd.kernel_spectrum(k2t, im2.shape)
+    o2 = torch.empty_like(i2)
+    ws2 = torch.empty(fcd.workspace_bytes(im2.shape, k2.shape), dtype=torch.uint8, device=dev)
+    ms_plain = _events_ms(torch, lambda: fcd.conv3d(i2, k2t, out=o2, workspace=ws2), 10, flush)
+    ms_reuse = _events_ms(torch, lambda: fcd.conv3d_kspec(i2, ks, k2.shape, out=o2, workspace=ws2), 10, flush)
+    fcd.conv3d_kspec(i2, ks, k2.shape, out=o2, workspace=ws2)
+    torch.cuda.synchronize()
+    out["kernel_spectrum_reuse"] = {
+        "workload": "plain_conv_512x512x128_psf31x31x63", "value": im2.size / (ms_reuse / 1e3) / 1e9,
+        "unit": "Gvoxel/s", "ms": ms_reuse, "plain_ms": ms_plain, "vs_plain": ms_plain / ms_reuse,
+        "fp64_rel_l2": _rel64(o2.cpu().numpy(), ref2)}
+    del i2, k2t, o2, ws2, ks
+    # Richardson-Lucy: 10 iterations on the 256^3 spot volume blurred by the 21^3 PSF
+    y3 = fcd.conv3d(torch.from_numpy(d["x_true"]).to(dev), torch.from_numpy(d["k_true"]).to(dev)).clamp_(min=0)
+    k3 = torch.from_numpy(d["k_true"]).to(dev)
+    iters = 10
+    est = torch.empty_like(y3)
+
+    def rl():
+        est.copy_(y3)
+        fcd.rl_deconvolve(y3, k3, iters, estimate=est)
+
+    ms_rl = _events_ms(torch, rl, 3, flush)
+    ms_c = _events_ms(torch, lambda: fcd.conv3d(y3, k3), 5, flush)
+    # FP64 restatement of the update, 2 iterations (numpy)
+    est.copy_(y3)
+    fcd.rl_deconvolve(y3, k3, 2, estimate=est)
+    torch.cuda.synchronize()
+    yn = y3.double().cpu().numpy()
+    _, pk3 = _fp64_conv(yn.astype(np.float32), d["k_true"])
+    K3 = np.fft.rfftn(pk3)
+    xr = yn.copy()
+    for _ in range(2):
+        e = np.fft.irfftn(np.fft.rfftn(xr) * K3, s=yn.shape, axes=(0, 1, 2))
+        r = np.divide(yn, e, out=np.zeros_like(yn), where=e > 0)
+        xr = xr * np.fft.irfftn(np.fft.rfftn(r) * np.conj(K3), s=yn.shape, axes=(0, 1, 2))
+    out["richardson_lucy"] = {
+        "workload": "rl_256x256x256_psf21x21x21_10_iterations", "value": y3.numel() * iters / (ms_rl / 1e3) / 1e9,
+        "unit": "Gvoxel-iterations/s", "ms": ms_rl, "ms_per_iteration": ms_rl / iters,
+        "plain_conv_ms": ms_c, "iteration_vs_two_plain_convs": 2 * ms_c / (ms_rl / iters),
+        "fp64_rel_l2_after_2_iterations": _rel64(est.cpu().numpy(), xr),
+        "how": "kernel spectrum once per call; per iteration conv and correlation against it + 2 pointwise passes"}
     return out
 
 

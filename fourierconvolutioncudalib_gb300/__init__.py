@@ -26,7 +26,7 @@ __all__ = [
     "selectDeviceWithHighestComputeCapability", "getCUDAcomputeCapabilityMajorVersion",
     "getCUDAcomputeCapabilityMinorVersion", "getNumDevicesCUDA", "getNameDeviceCUDA", "getMemDeviceCUDA",
     "cuda_version", "gpu_mem_needed_mb", "plan_radices",
-    "FC_FLAG_SHIFT_COMPAT", "FC_FLAG_DENSE_KERNEL", "FC_FLAG_TC_FP16", "FC_FLAG_TC_BF16",
+    "FC_FLAG_SHIFT_COMPAT", "FC_FLAG_DENSE_KERNEL", "FC_FLAG_TC_FP16", "FC_FLAG_TC_BF16", "FC_FLAG_CORRELATE",
 ]
 
 FC_OK, FC_ERR_ARG, FC_ERR_CUDA, FC_ERR_NOMEM, FC_ERR_UNSUPPORTED, FC_ERR_TIMEOUT = range(6)
@@ -34,6 +34,7 @@ FC_FLAG_SHIFT_COMPAT = 1
 FC_FLAG_DENSE_KERNEL = 2
 FC_FLAG_TC_FP16 = 4
 FC_FLAG_TC_BF16 = 8
+FC_FLAG_CORRELATE = 16
 
 _PKG = Path(__file__).resolve().parent
 LIB_NAME = "libFourierConvolutionCUDALib.so"
@@ -81,6 +82,12 @@ _SIGNATURES = {
     "fc_version": (ctypes.c_char_p, []),
     "fc_conv3d_workspace_bytes": (_SZ, [_IP, _IP, _I]),
     "fc_conv3d_device": (_I, [_P, _P, _IP, _P, _IP, _I, _P, _SZ, _P]),
+    "fc_kernel_spectrum_bytes": (_SZ, [_IP, _IP, _I]),
+    "fc_kernel_spectrum_device": (_I, [_P, _IP, _IP, _I, _P, _SZ, _P]),
+    "fc_conv3d_kspec_workspace_bytes": (_SZ, [_IP]),
+    "fc_conv3d_kspec_device": (_I, [_P, _P, _IP, _P, _IP, _I, _P, _SZ, _P]),
+    "fc_rl_workspace_bytes": (_SZ, [_IP, _IP, _I]),
+    "fc_rl_deconvolve_device": (_I, [_P, _P, _IP, _P, _IP, _I, _I, _P, _SZ, _P]),
     "fc_conv3d_adjoint_workspace_bytes": (_SZ, [_IP, _IP, _I]),
     "fc_conv3d_adjoint_device": (_I, [_P, _P, _P, _P, _P, _IP, _IP, _I, _P, _SZ, _P]),
     "fc_conv3d_batched_workspace_bytes": (_SZ, [_I, _IP, _I]),

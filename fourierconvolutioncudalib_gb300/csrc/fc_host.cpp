@@ -125,6 +125,9 @@ struct DevCtx {
   // side stream and events of the kernel-spectrum fork (created on first use)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // streams and events of the view-concurrent batched schedule (created on first use)
+  std::vector<cudaStream_t> bstreams;
+  std::vector<cudaEvent_t> bevents;
 };
 
 // The kernel-spectrum passes depend only on the kernel, so they can run on a
@@ -700,6 +703,87 @@ static void enqueue_adjoint(DevCtx& c, const Geom& g, const float* d_x, const fl
   }
 }
 
+// ------------------------------------------------------------------ kernel-spectrum reuse
+// The kernel's pruned xy-spectrum KXY ([kplanes][ny][pitch], plane p = image
+// plane (p - kz/2) mod nz) depends only on the kernel and the image shape.
+// Callers that convolve many images with one kernel (Richardson-Lucy
+// iterations, multi-view fusion) compute it once and then run only the five
+// image passes.  Buffer: KXY, then the KX rows used while computing it.
+static Layout kspec_layout(const Geom& g) {
+  Layout L;
+  const size_t row = (size_t)g.pitch * sizeof(float2);
+  L.off_KXY = 0;
+  size_t o = align256(row * g.ny * g.kplanes);
+  L.off_KX = o;
+  if (g.kbox) o = align256(o + row * g.krows * g.kplanes);
+  L.off_S = L.off_dense = L.off_aux = o;
+  L.total = o;
+  return L;
+}
+static size_t image_ws_bytes(const Geom& g) { return align256((size_t)g.pitch * sizeof(float2) * g.ny * g.nz); }
+
+static void enqueue_kspec(const Geom& g, const Axes& a, const float* d_kernel, char* kbuf, cudaStream_t st) {
+  const Tiles t = choose_tiles(g);
+  const Layout L = kspec_layout(g);
+  enqueue_kernel_x(g, a, t, d_kernel, kbuf, L, st);
+  enqueue_kernel_y(g, a, t, kbuf, L, 0, g.nxh, st);
+}
+
+// the five image passes against a ready kernel spectrum (conj: correlation)
+static void enqueue_conv_kspec(const Geom& g, const Axes& a, const float* d_image, float* d_out, const float2* KXY,
+                               bool conj, char* ws, cudaStream_t st) {
+  const Tiles t = choose_tiles(g);
+  float2* S = (float2*)ws;
+  const long long rows = (long long)g.ny * g.nz;
+  const long long ps = (long long)g.ny * g.pitch;
+  FC_PASS("image_x_r2c", 4.0 * g.N() + 8.0 * g.nxh * rows, st,
+          d_x_r2c_dense(d_image, g.nx, S, g.pitch, rows, a.x, t, st));
+  FC_PASS("image_y_fwd", 16.0 * g.nxh * (double)rows, st,
+          d_cols(S, S, ps, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2, t.threads, st));
+  FC_PASS(conj ? "zconv_conj" : "zconv", 16.0 * g.nxh * (double)rows + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
+          d_zconv(S, KXY, g.pitch, g.ny, g.nxh, g.kplanes, g.kbox ? g.kz / 2 : 0, 1.0f / (float)g.N(), conj, a.z,
+                  t.z_cols_log2, t.threads, st));
+  FC_PASS("image_y_inv", 16.0 * g.nxh * (double)rows, st,
+          d_cols(S, S, ps, g.pitch, g.nxh, g.nz, true, a.y, t.y_cols_log2, t.threads, st));
+  FC_PASS("image_x_c2r", 4.0 * g.N() + 8.0 * g.nxh * rows, st, d_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
+}
+
+// ------------------------------------------------------------------ Richardson-Lucy deconvolution
+// x <- x * correlate(y / conv(x, k), k), the multiplicative update for
+// Poisson data with a kernel of unit sum.  The kernel spectrum is computed
+// once per call; each iteration is two convolutions against it and two
+// pointwise passes.  Workspace: kernel spectrum, image spectrum, one volume.
+struct RlLayout {
+  size_t off_K, off_S, off_V, total;
+};
+static RlLayout rl_layout(const Geom& g) {
+  RlLayout L;
+  L.off_K = 0;
+  L.off_S = align256(kspec_layout(g).total);
+  L.off_V = align256(L.off_S + image_ws_bytes(g));
+  L.total = align256(L.off_V + sizeof(float) * (size_t)g.N());
+  return L;
+}
+
+static void enqueue_rl(DevCtx& c, const Geom& g, const float* d_y, float* d_x, const float* d_k, int iters,
+                       char* ws, size_t wsb, cudaStream_t st) {
+  const RlLayout L = rl_layout(g);
+  if (wsb < L.total) FC_THROW(FC_ERR_NOMEM, "workspace too small");
+  const Axes a = axes_for(c, g);
+  char* kbuf = ws + L.off_K;
+  const float2* KXY = (const float2*)(kbuf + kspec_layout(g).off_KXY);
+  char* S = ws + L.off_S;
+  float* V = (float*)(ws + L.off_V);
+  const long long n = g.N();
+  enqueue_kspec(g, a, d_k, kbuf, st);
+  for (int it = 0; it < iters; ++it) {
+    enqueue_conv_kspec(g, a, d_x, V, KXY, false, S, st);  // V = conv(x, k)
+    FC_PASS("rl_ratio", 12.0 * n, st, launch_rl_ratio(d_y, V, n, st));  // V = y / V
+    enqueue_conv_kspec(g, a, V, V, KXY, true, S, st);  // V = correlate(V, k)
+    FC_PASS("rl_update", 12.0 * n, st, launch_rl_update(d_x, V, n, st));  // x *= V
+  }
+}
+
 // ------------------------------------------------------------------ raw transforms
 static size_t fft_ws_bytes(const Geom& g) { return align256((size_t)g.pitch * sizeof(float2) * g.ny * g.nz); }
 
@@ -866,6 +950,7 @@ static void dims3(const int* d, int* a, int* b, int* cc) {
 // workspace, stream) into a CUDA graph and replayed.
 
 enum BChoice : int { kFatOcc = 0, kFatOne = 1, kPerView = 2 };
+constexpr int kBatchStreams = 4;  // streams of the view-concurrent schedule
 static const char* const kBPassName[5] = {"batch_x_r2c", "batch_y_fwd", "batch_zconv", "batch_y_inv", "batch_x_c2r"};
 
 struct BatchEntry {
@@ -879,7 +964,10 @@ struct BatchEntry {
   BTask* d_tasks = nullptr;
   size_t task_off[5] = {0, 0, 0, 0, 0};
   int choice[5] = {kFatOcc, kFatOcc, kFatOcc, kFatOcc, kFatOcc};
-  bool view_major = false;  // run each view's five passes in turn (its spectra stay in L2)
+  // 0: pass-major (one launch per pass over all views); 1: view-major (each
+  // view's passes in turn, its spectra stay in L2); 2: view-concurrent (the
+  // views' pass chains on kBatchStreams streams, parallel graph branches)
+  int schedule = 0;
   std::vector<std::vector<std::pair<int, int>>> view_tasks;  // per fast view: (pass, task index)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -1005,13 +1093,13 @@ static int sm_count() {
   return n;
 }
 
-static void launch_task(const BTask& t, int p, cudaStream_t st);
+static void launch_task(const BTask& t, int p, cudaStream_t st, bool pipe);
 
 static void launch_pass(BatchEntry& E, int p, int choice, cudaStream_t st) {
   const std::vector<BTask>& T = E.tasks[p];
   if (T.empty()) return;
   if (choice == kPerView) {
-    for (const BTask& t : T) launch_task(t, p, st);
+    for (const BTask& t : T) launch_task(t, p, st, true);
     return;
   }
   const BTask* d = E.d_tasks + E.task_off[p];
@@ -1038,8 +1126,10 @@ static void launch_pass(BatchEntry& E, int p, int choice, cudaStream_t st) {
   ++t_launches;
 }
 
-// one task on the single-volume kernel of its length
-static void launch_task(const BTask& t, int p, cudaStream_t st) {
+// one task on the single-volume kernel of its length; pipe: the pipelined x
+// kernels where they apply (not when views run concurrently: their CTAs take
+// a static share of the tiles and must all start together)
+static void launch_task(const BTask& t, int p, cudaStream_t st, bool pipe) {
   const FcAxis ax = task_axis(t);
   cudaError_t e = cudaSuccess;
   switch (t.mode) {
@@ -1047,10 +1137,16 @@ static void launch_task(const BTask& t, int p, cudaStream_t st) {
       e = fast_x_r2c_box((const float*)t.src, t.i0, t.i1, (float2*)t.dst, t.p1, t.rows, ax, st);
       break;
     case kBRowsDense:
-      e = fast_x_r2c_dense((const float*)t.src, t.p0, (float2*)t.dst, t.p1, t.rows, ax, st);
+      if (pipe && use_pipe() && aligned16(t.src) && t.p0 % 4 == 0)
+        e = pipe_x_r2c_dense((const float*)t.src, t.p0, (float2*)t.dst, t.p1, t.rows, ax, st);
+      else
+        e = fast_x_r2c_dense((const float*)t.src, t.p0, (float2*)t.dst, t.p1, t.rows, ax, st);
       break;
     case kBRowsC2R:
-      e = fast_x_c2r((const float2*)t.src, t.p0, (float*)t.dst, t.p1, t.rows, ax, st);
+      if (pipe && use_pipe() && aligned16(t.src) && t.p0 % 2 == 0)
+        e = pipe_x_c2r((const float2*)t.src, t.p0, (float*)t.dst, t.p1, t.rows, ax, st);
+      else
+        e = fast_x_c2r((const float2*)t.src, t.p0, (float*)t.dst, t.p1, t.rows, ax, st);
       break;
     case kBColsKX:
       e = fast_cols_kx((const float2*)t.src, t.p1, t.i0, t.i1, (float2*)t.dst, t.ncols, (int)t.rows, ax, st);
@@ -1073,9 +1169,30 @@ static void launch_task(const BTask& t, int p, cudaStream_t st) {
 
 static void run_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, float* const* outs,
                       const float* const* kers, char* ws, cudaStream_t st) {
-  if (E.view_major) {
+  if (E.schedule == 1) {
     for (const auto& vt : E.view_tasks)
-      for (const auto& pt : vt) launch_task(E.tasks[pt.first][pt.second], pt.first, st);
+      for (const auto& pt : vt) launch_task(E.tasks[pt.first][pt.second], pt.first, st, true);
+  } else if (E.schedule == 2) {
+    const int P = kBatchStreams;
+    while ((int)c.bstreams.size() < P) {
+      cudaStream_t s2;
+      cuda_check(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking), "cudaStreamCreate(batch)");
+      c.bstreams.push_back(s2);
+    }
+    while ((int)c.bevents.size() < P + 1) {
+      cudaEvent_t e2;
+      cuda_check(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming), "cudaEventCreate(batch)");
+      c.bevents.push_back(e2);
+    }
+    cuda_check(cudaEventRecord(c.bevents[P], st), "cudaEventRecord");
+    for (int i = 0; i < P; ++i) cuda_check(cudaStreamWaitEvent(c.bstreams[i], c.bevents[P], 0), "cudaStreamWaitEvent");
+    for (size_t v = 0; v < E.view_tasks.size(); ++v)
+      for (const auto& pt : E.view_tasks[v])
+        launch_task(E.tasks[pt.first][pt.second], pt.first, c.bstreams[v % P], false);
+    for (int i = 0; i < P; ++i) {
+      cuda_check(cudaEventRecord(c.bevents[i], c.bstreams[i]), "cudaEventRecord");
+      cuda_check(cudaStreamWaitEvent(st, c.bevents[i], 0), "cudaStreamWaitEvent");
+    }
   } else {
     for (int p = 0; p < 5; ++p) {
       PassScope ps(kBPassName[p], E.bytes[p], st);
@@ -1100,7 +1217,7 @@ static std::string tune_path() {
   return std::string(h ? h : ".") + "/.cache/fc_gb300_tune.txt";
 }
 
-static bool tune_lookup(const std::string& sig, int* choice, bool* view_major) {
+static bool tune_lookup(const std::string& sig, int* choice, int* schedule) {
   std::ifstream f(tune_path());
   std::string line;
   while (std::getline(f, line)) {
@@ -1113,13 +1230,14 @@ static bool tune_lookup(const std::string& sig, int* choice, bool* view_major) {
     for (int i = 0; i < 6; ++i) ok = ok && (bool)(is >> ch[i]);
     if (!ok) continue;
     for (int i = 0; i < 5; ++i) choice[i] = ch[i];
-    *view_major = ch[5] != 0;
+    if (ch[5] < 0 || ch[5] > 2) continue;
+    *schedule = ch[5];
     return true;
   }
   return false;
 }
 
-static void tune_store(const std::string& sig, const int* choice, bool view_major) {
+static void tune_store(const std::string& sig, const int* choice, int schedule) {
   const std::string path = tune_path();
   const size_t slash = path.find_last_of('/');
   if (slash != std::string::npos) {
@@ -1135,7 +1253,7 @@ static void tune_store(const std::string& sig, const int* choice, bool view_majo
   if (!f) return;
   f << sig;
   for (int i = 0; i < 5; ++i) f << ' ' << choice[i];
-  f << ' ' << (view_major ? 1 : 0) << '\n';
+  f << ' ' << schedule << '\n';
 }
 
 // on unless FC_AUTOTUNE=0
@@ -1177,10 +1295,11 @@ static void autotune_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, f
     }
     E.choice[p] = best_choice;
   }
-  // whole batch: the tuned pass-major schedule against the view-major one
-  float t_sched[2] = {1e30f, 1e30f};
-  for (int vm = 0; vm < 2; ++vm) {
-    E.view_major = vm == 1;
+  // whole batch: the tuned pass-major schedule against the view-major and view-concurrent ones
+  static const char* const kSchedName[3] = {"pass-major", "view-major", "view-concurrent"};
+  float t_sched[3] = {1e30f, 1e30f, 1e30f};
+  for (int sc = 0; sc < 3; ++sc) {
+    E.schedule = sc;
     for (int r = 0; r < 4; ++r) {
       cuda_check(cudaEventRecord(a, st), "cudaEventRecord");
       run_batch(c, E, imgs, outs, kers, ws, st);
@@ -1188,12 +1307,13 @@ static void autotune_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, f
       cuda_check(cudaEventSynchronize(b), "cudaEventSynchronize");
       float ms = 0.f;
       cudaEventElapsedTime(&ms, a, b);
-      if (r > 0) t_sched[vm] = std::min(t_sched[vm], ms);
+      if (r > 0) t_sched[sc] = std::min(t_sched[sc], ms);
     }
-    if (tune_log()) std::fprintf(stderr, "fc tune schedule %s: %.1f us\n", vm ? "view-major" : "pass-major",
-                                 1e3 * t_sched[vm]);
+    if (tune_log()) std::fprintf(stderr, "fc tune schedule %s: %.1f us\n", kSchedName[sc], 1e3 * t_sched[sc]);
   }
-  E.view_major = t_sched[1] < t_sched[0];
+  E.schedule = 0;
+  for (int sc = 1; sc < 3; ++sc)
+    if (t_sched[sc] < t_sched[E.schedule]) E.schedule = sc;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
 }
@@ -1207,7 +1327,7 @@ static std::string batch_signature(int nv, const int* dims) {
   for (char& ch : name)
     if (ch == ' ') ch = '_';
   std::ostringstream os;
-  os << name << ":v1";
+  os << name << ":v2";
   for (int i = 0; i < 6 * nv; ++i) os << (i % 6 == 0 ? ':' : 'x') << dims[i];
   return os.str();
 }
@@ -1281,9 +1401,9 @@ static void enqueue_batched(DevCtx& c, int nv, const float* const* imgs, float* 
                  "cudaMemcpy(work-list)");
     }
     const std::string sig = batch_signature(nv, dims);
-    if (!tune_lookup(sig, e->choice, &e->view_major) && autotune_enabled()) {
+    if (!tune_lookup(sig, e->choice, &e->schedule) && autotune_enabled()) {
       autotune_batch(c, *e, imgs, outs, kers, ws, st);
-      tune_store(sig, e->choice, e->view_major);
+      tune_store(sig, e->choice, e->schedule);
     }
     E = e.get();
     g_batch[key] = std::move(e);
@@ -1560,6 +1680,8 @@ int fc_release_device(int devCUDA) {
     if (c->side) cudaStreamDestroy(c->side);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    for (cudaStream_t s2 : c->bstreams) cudaStreamDestroy(s2);
+    for (cudaEvent_t e2 : c->bevents) cudaEventDestroy(e2);
     cudaSetDevice(prev);
   });
 }
@@ -1614,6 +1736,100 @@ size_t fc_conv3d_adjoint_workspace_bytes(const int* imDim, const int* kernelDim,
     r = adj_layout(make_geom(nx, ny, nz, kx, ky, kz, dense)).total;
   });
   return r;
+}
+
+// geometry of the kernel-spectrum entry points (no compat placement)
+static Geom kspec_geom(const int* imDim, const int* kernelDim, int flags) {
+  if (flags & FC_FLAG_SHIFT_COMPAT)
+    FC_THROW(FC_ERR_UNSUPPORTED, "kernel-spectrum entry points use the centred placement (no FC_FLAG_SHIFT_COMPAT)");
+  if ((flags & FC_FLAG_TC_FP16) && (flags & FC_FLAG_TC_BF16))
+    FC_THROW(FC_ERR_ARG, "choose one of FC_FLAG_TC_FP16 and FC_FLAG_TC_BF16");
+  int nx, ny, nz, kx = 0, ky = 0, kz = 0;
+  dims3(imDim, &nx, &ny, &nz);
+  const bool dense = flags & FC_FLAG_DENSE_KERNEL;
+  if (!dense) dims3(kernelDim, &kx, &ky, &kz);
+  return make_geom(nx, ny, nz, kx, ky, kz, dense);
+}
+struct TcFlags {
+  explicit TcFlags(int flags) { t_tc_mode = (flags & FC_FLAG_TC_FP16) ? 1 : (flags & FC_FLAG_TC_BF16) ? 2 : 0; }
+  ~TcFlags() { t_tc_mode = 0; }
+};
+static void check_align256(const void* p, const char* what) {
+  if (((uintptr_t)p & 255) != 0) FC_THROW(FC_ERR_ARG, std::string(what) + " must be 256-byte aligned");
+}
+
+size_t fc_kernel_spectrum_bytes(const int* imDim, const int* kernelDim, int flags) {
+  clear_status();
+  size_t r = 0;
+  guarded([&] { r = kspec_layout(kspec_geom(imDim, kernelDim, flags)).total; });
+  return r;
+}
+
+int fc_kernel_spectrum_device(const float* d_kernel, const int* kernelDim, const int* imDim, int flags, void* d_kspec,
+                              size_t kspec_bytes, void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_kernel || !d_kspec) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    const Geom g = kspec_geom(imDim, kernelDim, flags);
+    if (kspec_bytes < kspec_layout(g).total) FC_THROW(FC_ERR_NOMEM, "kernel-spectrum buffer too small");
+    check_align256(d_kspec, "kernel-spectrum buffer");
+    TcFlags tc(flags);
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    enqueue_kspec(g, axes_for(c, g), d_kernel, (char*)d_kspec, (cudaStream_t)stream);
+  });
+}
+
+size_t fc_conv3d_kspec_workspace_bytes(const int* imDim) {
+  clear_status();
+  size_t r = 0;
+  guarded([&] {
+    int nx, ny, nz;
+    dims3(imDim, &nx, &ny, &nz);
+    r = image_ws_bytes(make_geom(nx, ny, nz, 1, 1, 1, false));
+  });
+  return r;
+}
+
+int fc_conv3d_kspec_device(const float* d_image, float* d_out, const int* imDim, const void* d_kspec,
+                           const int* kernelDim, int flags, void* d_workspace, size_t workspace_bytes, void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_image || !d_out || !d_kspec) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    const Geom g = kspec_geom(imDim, kernelDim, flags);
+    check_align256(d_kspec, "kernel-spectrum buffer");
+    TcFlags tc(flags);
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t wsb = workspace_bytes;
+    void* ws = resolve_ws(c, d_workspace, &wsb, image_ws_bytes(g));
+    enqueue_conv_kspec(g, axes_for(c, g), d_image, d_out, (const float2*)((const char*)d_kspec + kspec_layout(g).off_KXY),
+                       (flags & FC_FLAG_CORRELATE) != 0, (char*)ws, (cudaStream_t)stream);
+  });
+}
+
+size_t fc_rl_workspace_bytes(const int* imDim, const int* kernelDim, int flags) {
+  clear_status();
+  size_t r = 0;
+  guarded([&] { r = rl_layout(kspec_geom(imDim, kernelDim, flags)).total; });
+  return r;
+}
+
+int fc_rl_deconvolve_device(const float* d_observed, float* d_estimate, const int* imDim, const float* d_kernel,
+                            const int* kernelDim, int iterations, int flags, void* d_workspace, size_t workspace_bytes,
+                            void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_observed || !d_estimate || !d_kernel) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    if (iterations < 0) FC_THROW(FC_ERR_ARG, "iterations must be >= 0");
+    const Geom g = kspec_geom(imDim, kernelDim, flags);
+    TcFlags tc(flags);
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t wsb = workspace_bytes;
+    void* ws = resolve_ws(c, d_workspace, &wsb, rl_layout(g).total);
+    enqueue_rl(c, g, d_observed, d_estimate, d_kernel, iterations, (char*)ws, wsb, (cudaStream_t)stream);
+  });
 }
 
 int fc_conv3d_adjoint_device(const float* d_image, const float* d_kernel, const float* d_grad_out,

@@ -71,6 +71,10 @@ cudaError_t launch_pad_shift(const float* taps, int kx, int ky, int kz, int nx, 
 // Crop/gather for the kernel gradient: out[iz][iy][ix] = vol[(iz-hz)%nz][(iy-hy)%ny][(ix-hx)%nx]
 // from a real volume whose rows have `pitch` floats and whose planes are
 // given by a compact array of kz planes (plane p holds z = (p - hz) mod nz).
+// Richardson-Lucy pointwise steps over n floats: v = y / v where v > 0 (else
+// 0); x = x * v
+cudaError_t launch_rl_ratio(const float* y, float* v, long long n, cudaStream_t st);
+cudaError_t launch_rl_update(float* x, const float* v, long long n, cudaStream_t st);
 cudaError_t launch_crop_kernel(const float* vol, long long row_pitch, int ny_rows, int nx, int kx, int ky, int kz,
                                float* out, cudaStream_t st);
 

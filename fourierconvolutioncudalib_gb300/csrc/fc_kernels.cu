@@ -12,6 +12,8 @@
 // The kernel's zero padding and centre shift (the reference's fftShiftKernel,
 // src/convolution3Dfft.cu:128-166) is folded into the loads of the kernel's x
 // pass: only the rows and planes that hold taps are transformed.
+#include <algorithm>
+
 #include "fc_internal.h"
 #include "fc_fft.cuh"
 #include "fc_sources.cuh"
@@ -433,6 +435,72 @@ cudaError_t launch_pad_shift(const float* taps, int kx, int ky, int kz, int nx, 
     const unsigned grid = (unsigned)((covered + 255) / 256 < 65535 ? (covered + 255) / 256 : 65535);
     k_pad_shift_compat<<<grid, 256, 0, st>>>(taps, kx, ky, kz, nx, ny, nz, covered, out);
   }
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ Richardson-Lucy pointwise steps
+__device__ __forceinline__ float rl_ratio1(float y, float e) { return e > 0.f ? y / e : 0.f; }
+
+__global__ void k_rl_ratio(const float* __restrict__ y, float* __restrict__ v, long long n, bool vec) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long done = 0;
+  if (vec) {
+    const long long n4 = n / 4;
+    const float4* y4 = reinterpret_cast<const float4*>(y);
+    float4* v4 = reinterpret_cast<float4*>(v);
+    for (long long i = i0; i < n4; i += stride) {
+      const float4 a = y4[i];
+      float4 e = v4[i];
+      e.x = rl_ratio1(a.x, e.x);
+      e.y = rl_ratio1(a.y, e.y);
+      e.z = rl_ratio1(a.z, e.z);
+      e.w = rl_ratio1(a.w, e.w);
+      v4[i] = e;
+    }
+    done = n4 * 4;
+  }
+  for (long long i = done + i0; i < n; i += stride) v[i] = rl_ratio1(y[i], v[i]);
+}
+
+__global__ void k_rl_update(float* __restrict__ x, const float* __restrict__ v, long long n, bool vec) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long done = 0;
+  if (vec) {
+    const long long n4 = n / 4;
+    float4* x4 = reinterpret_cast<float4*>(x);
+    const float4* v4 = reinterpret_cast<const float4*>(v);
+    for (long long i = i0; i < n4; i += stride) {
+      float4 a = x4[i];
+      const float4 c = v4[i];
+      a.x *= c.x;
+      a.y *= c.y;
+      a.z *= c.z;
+      a.w *= c.w;
+      x4[i] = a;
+    }
+    done = n4 * 4;
+  }
+  for (long long i = done + i0; i < n; i += stride) x[i] *= v[i];
+}
+
+static unsigned pointwise_grid(long long n) {
+  const long long b = (n / 4 + 255) / 256;
+  return (unsigned)std::max<long long>(1, std::min<long long>(b, 152LL * 16));
+}
+
+cudaError_t launch_rl_ratio(const float* y, float* v, long long n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const bool vec = (((uintptr_t)y | (uintptr_t)v) & 15) == 0;
+  k_rl_ratio<<<pointwise_grid(n), 256, 0, st>>>(y, v, n, vec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rl_update(float* x, const float* v, long long n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const bool vec = (((uintptr_t)x | (uintptr_t)v) & 15) == 0;
+  k_rl_update<<<pointwise_grid(n), 256, 0, st>>>(x, v, n, vec);
   return cudaGetLastError();
 }
 

@@ -12,10 +12,10 @@ from typing import List, Optional, Sequence, Tuple
 
 import torch
 
-from . import FC_FLAG_DENSE_KERNEL, FcError, FC_ERR_ARG, _check, _iarr, lib
+from . import FC_FLAG_CORRELATE, FC_FLAG_DENSE_KERNEL, FcError, FC_ERR_ARG, _check, _iarr, lib
 
 __all__ = ["conv3d", "conv3d_adjoint", "conv3d_batched", "rfft3d", "irfft3d", "pad_shift_kernel",
-           "workspace_bytes", "profile", "launch_count"]
+           "kernel_spectrum", "conv3d_kspec", "rl_deconvolve", "workspace_bytes", "profile", "launch_count"]
 
 
 def _dims(t: torch.Tensor) -> Tuple[int, int, int]:
@@ -77,6 +77,70 @@ def conv3d(image: torch.Tensor, kernel: torch.Tensor, out: Optional[torch.Tensor
                                 int(flags), wp, wb, _stream(stream))
     _check(rc)
     return out
+
+
+def _kdims(kernel_shape: Optional[Sequence[int]], flags: int):
+    if flags & FC_FLAG_DENSE_KERNEL:
+        return None
+    kz, ky, kx = kernel_shape
+    return _iarr([kx, ky, kz])
+
+
+def kernel_spectrum(kernel: torch.Tensor, image_shape: Sequence[int], flags: int = 0,
+                    stream: Optional[torch.cuda.Stream] = None) -> torch.Tensor:
+    """The kernel's spectrum for images of image_shape (z, y, x), as an opaque
+    device buffer for conv3d_kspec / reuse across calls."""
+    _f32(kernel, "kernel")
+    nz, ny, nx = image_shape
+    kd = _kdims(tuple(kernel.shape), flags)
+    need = lib().fc_kernel_spectrum_bytes(_iarr([nx, ny, nz]), kd, int(flags))
+    if need == 0:
+        _check()
+    buf = torch.empty(need, dtype=torch.uint8, device=kernel.device)
+    _check(lib().fc_kernel_spectrum_device(kernel.data_ptr(), kd, _iarr([nx, ny, nz]), int(flags), buf.data_ptr(),
+                                           need, _stream(stream)))
+    return buf
+
+
+def conv3d_kspec(image: torch.Tensor, kspec: torch.Tensor, kernel_shape: Optional[Sequence[int]],
+                 out: Optional[torch.Tensor] = None, correlate: bool = False, flags: int = 0,
+                 workspace: Optional[torch.Tensor] = None, stream: Optional[torch.cuda.Stream] = None) -> torch.Tensor:
+    """Convolution (or correlation) of image with a kernel spectrum from kernel_spectrum()."""
+    _f32(image, "image")
+    nx, ny, nz = _dims(image)
+    if out is None:
+        out = torch.empty_like(image)
+    _f32(out, "out")
+    if correlate:
+        flags |= FC_FLAG_CORRELATE
+    need = lib().fc_conv3d_kspec_workspace_bytes(_iarr([nx, ny, nz]))
+    if need == 0:
+        _check()
+    wp, wb = _ws(workspace, need, image.device)
+    _check(lib().fc_conv3d_kspec_device(image.data_ptr(), out.data_ptr(), _iarr([nx, ny, nz]), kspec.data_ptr(),
+                                        _kdims(kernel_shape, flags), int(flags), wp, wb, _stream(stream)))
+    return out
+
+
+def rl_deconvolve(observed: torch.Tensor, kernel: torch.Tensor, iterations: int,
+                  estimate: Optional[torch.Tensor] = None, flags: int = 0, workspace: Optional[torch.Tensor] = None,
+                  stream: Optional[torch.cuda.Stream] = None) -> torch.Tensor:
+    """Richardson-Lucy deconvolution of observed [nz,ny,nx] by kernel [kz,ky,kx];
+    estimate (updated in place) starts as a copy of observed when not given."""
+    _f32(observed, "observed")
+    _f32(kernel, "kernel")
+    nx, ny, nz = _dims(observed)
+    if estimate is None:
+        estimate = observed.clone()
+    _f32(estimate, "estimate")
+    kd = _kdims(tuple(kernel.shape), flags)
+    need = lib().fc_rl_workspace_bytes(_iarr([nx, ny, nz]), kd, int(flags))
+    if need == 0:
+        _check()
+    wp, wb = _ws(workspace, need, observed.device)
+    _check(lib().fc_rl_deconvolve_device(observed.data_ptr(), estimate.data_ptr(), _iarr([nx, ny, nz]),
+                                         kernel.data_ptr(), kd, int(iterations), int(flags), wp, wb, _stream(stream)))
+    return estimate
 
 
 def conv3d_adjoint(image: Optional[torch.Tensor], kernel: Optional[torch.Tensor], grad_out: torch.Tensor,

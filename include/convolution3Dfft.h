@@ -93,6 +93,8 @@ FUNCTION_PREFIX int gpu_mem_needed_mb(int* shape, int len);
 #define FC_FLAG_DENSE_KERNEL 2 /* kernel is an image-sized, already shifted array of N floats */
 #define FC_FLAG_TC_FP16 4      /* tensor-core DFT stages, fp16 hi+lo split operands, fp32 accumulate */
 #define FC_FLAG_TC_BF16 8      /* tensor-core DFT stages, bf16 hi+lo split operands, fp32 accumulate */
+#define FC_FLAG_CORRELATE 16   /* fc_conv3d_kspec_device: multiply by the conjugate kernel spectrum, i.e.
+                                  convolve with the kernel flipped about its centre (the adjoint) */
 
 FUNCTION_PREFIX int fc_last_status(void);
 FUNCTION_PREFIX const char* fc_last_error(void);
@@ -171,6 +173,36 @@ FUNCTION_PREFIX int fc_pad_shift_kernel_device(const float* d_kernel, const int*
 /* Radix plan of a transform length, for inspection: writes up to max_stages
  * radices and returns their count (or -1). Host-only, needs no GPU. */
 FUNCTION_PREFIX int fc_plan_radices(int n, int* radices, int max_stages);
+
+/* Kernel-spectrum reuse (no reference counterpart; the reference recomputes
+ * the kernel's FFT on every call, its TODO at src/convolution3Dfft.cu:363).
+ * fc_kernel_spectrum_device writes the kernel's spectrum for images of imDim
+ * into a caller buffer of fc_kernel_spectrum_bytes (256-byte aligned; the
+ * centred placement, flags FC_FLAG_DENSE_KERNEL / FC_FLAG_TC_* as for
+ * fc_conv3d_device); fc_conv3d_kspec_device then convolves any number of
+ * images with it, running only the image passes (FC_FLAG_CORRELATE:
+ * correlation, i.e. the kernel flipped about its centre).  Workspace:
+ * fc_conv3d_kspec_workspace_bytes, or NULL for the library's own.  Both
+ * are asynchronous on `stream`. */
+FUNCTION_PREFIX size_t fc_kernel_spectrum_bytes(const int* imDim, const int* kernelDim, int flags);
+FUNCTION_PREFIX int fc_kernel_spectrum_device(const float* d_kernel, const int* kernelDim, const int* imDim, int flags,
+                                              void* d_kspec, size_t kspec_bytes, void* stream);
+FUNCTION_PREFIX size_t fc_conv3d_kspec_workspace_bytes(const int* imDim);
+FUNCTION_PREFIX int fc_conv3d_kspec_device(const float* d_image, float* d_out, const int* imDim, const void* d_kspec,
+                                           const int* kernelDim, int flags, void* d_workspace, size_t workspace_bytes,
+                                           void* stream);
+
+/* Richardson-Lucy deconvolution (no reference counterpart; the operator's
+ * consumer named for this library): `iterations` updates
+ * x <- x * correlate(y / conv(x, k), k) of the estimate d_estimate (holds the
+ * starting estimate on entry, e.g. a copy of y), for a non-negative kernel of
+ * unit sum; where conv(x, k) <= 0 the ratio is 0.  The kernel spectrum is
+ * computed once per call.  Workspace: fc_rl_workspace_bytes, or NULL for the
+ * library's own.  Asynchronous on `stream`. */
+FUNCTION_PREFIX size_t fc_rl_workspace_bytes(const int* imDim, const int* kernelDim, int flags);
+FUNCTION_PREFIX int fc_rl_deconvolve_device(const float* d_observed, float* d_estimate, const int* imDim,
+                                            const float* d_kernel, const int* kernelDim, int iterations, int flags,
+                                            void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* Per-pass timing: when enabled, every pass records CUDA events on the stream
  * it is launched on.  fc_profile_read synchronises and copies up to max

@@ -211,6 +211,30 @@ def conv_fp64(image: np.ndarray, kernel: np.ndarray, placement: str = "centered"
     return fft_conv_fp64(image, pk)
 
 
+def correlate_fp64(image: np.ndarray, kernel: np.ndarray) -> np.ndarray:
+    """FP64 circular correlation with the centred kernel: the conjugate kernel
+    spectrum, i.e. convolution with the kernel flipped about its centre."""
+    pk = centered_padded_kernel(kernel, image.shape).astype(np.float64)
+    a = np.fft.rfftn(np.asarray(image, np.float64))
+    return np.fft.irfftn(a * np.conj(np.fft.rfftn(pk)), s=image.shape, axes=(0, 1, 2))
+
+
+def rl_fp64(observed: np.ndarray, kernel: np.ndarray, iterations: int,
+            estimate: Optional[np.ndarray] = None) -> np.ndarray:
+    """Richardson-Lucy deconvolution in double precision (the published
+    multiplicative update of Richardson 1972 / Lucy 1974; no reference
+    counterpart): x <- x * correlate(y / conv(x, k), k) with the centred
+    circular placement, ratio 0 where conv(x, k) <= 0."""
+    y = np.asarray(observed, np.float64)
+    K = np.fft.rfftn(centered_padded_kernel(kernel, y.shape).astype(np.float64))
+    x = (y if estimate is None else np.asarray(estimate, np.float64)).copy()
+    for _ in range(iterations):
+        est = np.fft.irfftn(np.fft.rfftn(x) * K, s=y.shape, axes=(0, 1, 2))
+        ratio = np.divide(y, est, out=np.zeros_like(y), where=est > 0)
+        x = x * np.fft.irfftn(np.fft.rfftn(ratio) * np.conj(K), s=y.shape, axes=(0, 1, 2))
+    return x
+
+
 def reference_path_fp32(image: np.ndarray, kernel: np.ndarray, placement: str = "centered",
                         workers: int = -1) -> np.ndarray:
     """The reference's InPlace algorithm on the host in float32:

@@ -111,6 +111,36 @@ def test_batched_autotune_cache(cuda, orc, tmp_path):
                 os.environ[k] = v
     text = cache.read_text().strip().splitlines()
     assert len(text) == 1 and len(text[0].split()) == 7
-    assert all(c in "012" for c in text[0].split()[1:6]) and text[0].split()[6] in "01"
+    assert all(c in "012" for c in text[0].split()[1:6]) and text[0].split()[6] in "012"
     for (im, k), out in zip(views, outs):
         assert _rel(out.cpu().numpy(), orc.conv_fp64(im, k, "centered")) <= 1e-5
+
+
+def test_batched_every_schedule_and_choice(cuda, orc, tmp_path):
+    """Each schedule (pass-major, view-major, view-concurrent) with the
+    persistent work-list launches and with one launch per view, forced through
+    the tuning cache; every view against the FP64 oracle."""
+    rng = np.random.default_rng(9)
+    views = _views(rng, [((16, 48, 96), (3, 5, 7)), ((20, 64, 128), (5, 5, 5)), ((24, 40, 64), (5, 7, 9))])
+    cache = tmp_path / "tune.txt"
+    old = {k: os.environ.get(k) for k in ("FC_AUTOTUNE", "FC_TUNE_CACHE")}
+    keep = []  # earlier buffers stay allocated, so every run gets new pointers and a new graph entry
+    try:
+        os.environ["FC_TUNE_CACHE"] = str(cache)
+        os.environ["FC_AUTOTUNE"] = "1"
+        keep.append(_run_batched(cuda, views))
+        sig = cache.read_text().split()[0]
+        os.environ["FC_AUTOTUNE"] = "0"
+        for sched in (0, 1, 2):
+            for choice in (0, 2):
+                cache.write_text(" ".join([sig] + [str(choice)] * 5 + [str(sched)]) + "\n")
+                imgs, kers, outs = _run_batched(cuda, views)
+                keep.append((imgs, kers, outs))
+                for (im, k), out in zip(views, outs):
+                    assert _rel(out.cpu().numpy(), orc.conv_fp64(im, k, "centered")) <= 1e-5, (sched, choice)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v

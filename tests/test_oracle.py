@@ -141,3 +141,21 @@ def test_metrics(orc):
     b = a + np.float32(0.1)
     assert abs(orc.l2norm(a, b) - np.sqrt(100 * 0.1 ** 2) / 100) < 1e-7
     assert abs(orc.l2norm_by_nvidia(a, b) - np.sqrt(100 * 0.01) / np.sqrt(100 * 1.1 ** 2)) < 1e-6
+
+
+def test_rl_oracle_conserves_flux_and_sharpens(orc):
+    """The FP64 Richardson-Lucy restatement: with a unit-sum kernel and a
+    positive estimate the update keeps sum(x) = sum(y), and it moves a
+    blurred pair of spots back towards the spots."""
+    rng = np.random.default_rng(1)
+    truth = np.ones((16, 20, 24))
+    truth[8, 10, 12] = 500.0
+    truth[3, 4, 5] = 200.0
+    k = rng.random((5, 3, 7))
+    k = (k / k.sum()).astype(np.float32)
+    y = orc.conv_fp64(truth, k, "centered")
+    x = orc.rl_fp64(y, k, 20)
+    assert abs(x.sum() / y.sum() - 1) < 1e-12
+    err = lambda a: np.linalg.norm(a - truth) / np.linalg.norm(truth)
+    assert err(x) < 0.5 * err(y)
+    assert np.allclose(orc.correlate_fp64(y, k), orc.conv_fp64(y, np.ascontiguousarray(k[::-1, ::-1, ::-1]), "centered"))
