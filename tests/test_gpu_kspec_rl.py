@@ -86,7 +86,9 @@ def test_kspec_rejects_compat_and_small_buffer(cuda):
     assert rc == fc.FC_ERR_NOMEM
 
 
-@pytest.mark.parametrize("shape,kshape", [((32, 48, 40), (9, 5, 7)), ((24, 40, 56), (5, 7, 3))])
+# x extents 40 and 56 run on the generic kernels, 64 and 96 on the register-resident ones
+@pytest.mark.parametrize("shape,kshape", [((32, 48, 40), (9, 5, 7)), ((24, 40, 56), (5, 7, 3)),
+                                          ((32, 48, 64), (9, 5, 7)), ((20, 32, 96), (5, 7, 9))])
 def test_richardson_lucy_vs_fp64(cuda, orc, shape, kshape):
     import torch
     from fourierconvolutioncudalib_gb300 import device as fcd
