@@ -97,6 +97,44 @@ cudaError_t fast_cols(const float2* src, float2* dst, long long ps, long long es
                  : fast::dispatch_cols<false>(ax.n, s, dst, ps, es, ncols, nplanes, ax.W, st);
 }
 
+namespace fast {
+template <int N, bool INV>
+static cudaError_t run_cols_wide(float2* S, long long ps, long long es, int ncols, int nplanes, const float2* W,
+                                 cudaStream_t st) {
+  using G = ColGeomWide<N>;
+  // measured on GB300: wider tiles pay off for columns of 1024 (32-byte row
+  // segments otherwise) and cost time at 512 and below
+  if constexpr (G::B == ColGeom<N>::B || N < 1024) {
+    return run_cols<N, INV, ColPlain>(ColPlain{S, ps, es}, S, ps, es, ncols, nplanes, W, st);
+  } else {
+    constexpr int sm = G::SMEM * (int)sizeof(float2);
+    if (sm > 48 * 1024) {
+      const cudaError_t e =
+          cudaFuncSetAttribute(k_cols_wide<N, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      if (e != cudaSuccess) return e;
+    }
+    const dim3 grid((ncols + G::B - 1) / G::B, nplanes);
+    k_cols_wide<N, INV><<<grid, G::THREADS, sm, st>>>(S, ps, es, ncols, W);
+    return cudaGetLastError();
+  }
+}
+}  // namespace fast
+
+cudaError_t fast_cols_wide(float2* S, long long ps, long long es, int ncols, int nplanes, bool inverse,
+                           const FcAxis& ax, cudaStream_t st) {
+  if (nplanes <= 0 || ncols <= 0) return cudaSuccess;
+  switch (ax.n) {
+#define FC_CASE(n_)                                                                      \
+  case n_:                                                                               \
+    return inverse ? fast::run_cols_wide<n_, true>(S, ps, es, ncols, nplanes, ax.W, st)  \
+                   : fast::run_cols_wide<n_, false>(S, ps, es, ncols, nplanes, ax.W, st);
+    FC_COL_SIZES(FC_CASE)
+#undef FC_CASE
+    default:
+      return cudaErrorNotSupported;
+  }
+}
+
 cudaError_t fast_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
                          int nplanes, const FcAxis& ax, cudaStream_t st) {
   if (nplanes <= 0 || ncols <= 0) return cudaSuccess;

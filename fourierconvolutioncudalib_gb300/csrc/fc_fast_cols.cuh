@@ -21,12 +21,12 @@
 namespace fc {
 namespace fast {
 
-// columns per tile: the largest power of two <= BMAX with N*B <= 4096 values
-// and B*T <= 256 threads (4 at least)
-template <int N, int BMAX = 32>
+// columns per tile: the largest power of two <= BMAX with N*B <= VMAX values
+// and B*T <= TMAX threads (4 at least)
+template <int N, int BMAX = 32, int TMAX = 256, int VMAX = 4096>
 struct ColGeomB {
   static constexpr int T = Plan<N>::T;
-  static constexpr int B0a = 4096 / N, B0b = 256 / T;
+  static constexpr int B0a = VMAX / N, B0b = TMAX / T;
   static constexpr int B0 = (B0a < B0b ? B0a : B0b) < BMAX ? (B0a < B0b ? B0a : B0b) : BMAX;
   static constexpr int B = B0 >= 32 ? 32 : B0 >= 16 ? 16 : B0 >= 8 ? 8 : 4;
   static constexpr int THREADS = B * T;
@@ -34,13 +34,17 @@ struct ColGeomB {
 };
 template <int N>
 using ColGeom = ColGeomB<N, 32>;
+// wide tiles for the image y passes: up to 512 threads and 8192 values, so that
+// long columns still read rows of 8-16 columns (64-128 contiguous bytes);
+// the exchange tile then needs dynamic shared memory
+template <int N>
+using ColGeomWide = ColGeomB<N, 32, 512, 8192>;
 
 // y pass body: tile (bx, plane) = columns [bx*B, bx*B + B) of one plane.
-template <int N, bool INV, class Src, int TCM = tc::kNone>
+template <int N, bool INV, class Src, int TCM = tc::kNone, class G = ColGeom<N>>
 __device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long ps, long long es, int ncols,
                                           const float2* __restrict__ W, int bx, int plane, int tid, float2* sm,
                                           const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
-  using G = ColGeom<N>;
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, INV>(), RF = last_radix<N, INV>();
   const int c = tid % B;
@@ -62,6 +66,15 @@ __device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long
       if (j >= 0) d[(long long)j * es] = v[q];
     }
   }
+}
+
+// y pass on wide tiles (dynamic shared memory of ColGeomWide<N>::SMEM float2)
+template <int N, bool INV>
+__global__ void __launch_bounds__(ColGeomWide<N>::THREADS, 1024 / ColGeomWide<N>::THREADS) k_cols_wide(float2* S, long long ps, long long es,
+                                                                       int ncols, const float2* __restrict__ W) {
+  extern __shared__ __align__(16) float2 wsm[];
+  body_cols<N, INV, ColPlain, tc::kNone, ColGeomWide<N>>(ColPlain{S, ps, es}, S, ps, es, ncols, W, (int)blockIdx.x,
+                                                         (int)blockIdx.y, (int)threadIdx.x, wsm);
 }
 
 template <int N, bool INV, class Src>

@@ -371,6 +371,15 @@ static bool use_pipe() {
   }
   return g_pipe != 0;
 }
+// in-place y passes on wide tiles (FC_COLS_WIDE=0: the 256-thread tiles)
+static int g_cols_wide = -1;
+static bool cols_wide() {
+  if (g_cols_wide < 0) {
+    const char* e = std::getenv("FC_COLS_WIDE");
+    g_cols_wide = e ? std::atoi(e) : 1;
+  }
+  return g_cols_wide != 0;
+}
 // set while the enqueue in progress on this thread reads the image from host memory
 static thread_local bool t_host_src = false;
 struct HostSrcScope {
@@ -408,7 +417,10 @@ static cudaError_t d_cols(const float2* src, float2* dst, long long ps, long lon
                           const FcAxis& ax, int cols_log2, int threads, cudaStream_t st) {
   if (t_tc_mode && tc_len(ax.n))
     return FC_TC_CALL(tc_cols, inv ? 1 : 0, src, 0, 0, 0, dst, ps, es, ncols, nplanes, ax, st);
-  if (use_fast() && fast_cols_supported(ax.n)) return fast_cols(src, dst, ps, es, ncols, nplanes, inv, ax, st);
+  if (use_fast() && fast_cols_supported(ax.n)) {
+    if (src == dst && cols_wide()) return fast_cols_wide(dst, ps, es, ncols, nplanes, inv, ax, st);
+    return fast_cols(src, dst, ps, es, ncols, nplanes, inv, ax, st);
+  }
   return launch_cols(src, dst, ps, es, ncols, nplanes, inv, ax, cols_log2, threads, st);
 }
 static cudaError_t d_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,

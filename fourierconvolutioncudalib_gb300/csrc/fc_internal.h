@@ -107,6 +107,9 @@ cudaError_t pipe_x_r2c_dense(const float* in, long long in_pitch, float2* out, l
 cudaError_t pipe_x_c2r(const float2* in, long long in_pitch, float* out, long long out_pitch, long long nrows,
                        const FcAxis& ax, cudaStream_t st);
 unsigned int pipe_take_timeouts();
+// in-place y pass on wide tiles (fast::ColGeomWide)
+cudaError_t fast_cols_wide(float2* S, long long ps, long long es, int ncols, int nplanes, bool inverse,
+                           const FcAxis& ax, cudaStream_t st);
 cudaError_t fast_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
                          int nplanes, const FcAxis& ax, cudaStream_t st);
 cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
