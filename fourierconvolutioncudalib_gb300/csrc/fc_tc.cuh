@@ -29,8 +29,10 @@ constexpr int kNone = 0, kFp16 = 1, kBf16 = 2;
 // the 32 x 33-float output tile
 constexpr int kColWords = 17;
 constexpr int kWarpWords = 2 * 32 * kColWords;  // 1088 words (>= 32*33 floats)
-// per-CTA table of the A fragments: [dir 2][i 2][kk 2][lane 32][4 regs] x (hi, lo)
-constexpr int kTableWords = 2 * 2 * 2 * 32 * 4 * 2;  // 1024 words
+// per-CTA table of the A fragments of the two distinct 16 x 16 blocks of the
+// real DFT matrix, C[r][c] = cos(2 pi r c / 16) and S[r][c] = sin(2 pi r c / 16):
+// [block 2][lane 32][4 regs] x (hi, lo)
+constexpr int kTableWords = 2 * 32 * 4 * 2;  // 512 words
 
 template <int TCM>
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
@@ -79,27 +81,18 @@ __device__ __forceinline__ float cos16(int k) {
   return a <= 4 ? c : -c;
 }
 
-// entry (r, c) of the real 32 x 32 DFT matrix; dir 0 forward (exp(-i...)), 1 inverse
-__device__ __forceinline__ float dft_real(int r, int c, int dir) {
-  const int k = (r & 15) * (c & 15);
-  const float cs = cos16(k);
-  const float sn = cos16(k - 4);  // sin(2 pi k / 16) = cos(2 pi (k - 4) / 16)
-  const float im = dir ? sn : -sn;  // Im W
-  if (r < 16) return (c < 16) ? cs : -im;
-  return (c < 16) ? im : cs;
-}
-
 // Fill the A-fragment table (call with all threads of the CTA, then barrier).
+// Fragment layout of m16n8k16 (row-major A): register reg of lane (g = lane/4,
+// q = lane%4) holds A[g + 8*(reg&1)][2q + 8*(reg>>1) + {0,1}].
 template <int TCM>
 __device__ __forceinline__ void build_table(uint32_t* tab, int tid, int nthreads) {
-  for (int e = tid; e < 2 * 2 * 2 * 32; e += nthreads) {
-    const int lane = e & 31, kk = (e >> 5) & 1, i = (e >> 6) & 1, dir = e >> 7;
+  for (int e = tid; e < 2 * 32; e += nthreads) {
+    const int lane = e & 31, blk = e >> 5;  // blk 0: C, 1: S
     const int g = lane >> 2, q = lane & 3;
-    const int rows[4] = {16 * i + g, 16 * i + g + 8, 16 * i + g, 16 * i + g + 8};
-    const int cols[4] = {16 * kk + 2 * q, 16 * kk + 2 * q, 16 * kk + 2 * q + 8, 16 * kk + 2 * q + 8};
     for (int reg = 0; reg < 4; ++reg) {
-      const float f0 = dft_real(rows[reg], cols[reg], dir);
-      const float f1 = dft_real(rows[reg], cols[reg] + 1, dir);
+      const int r = g + 8 * (reg & 1), c = 2 * q + 8 * (reg >> 1);
+      const float f0 = blk ? cos16(r * c - 4) : cos16(r * c);  // sin(x) = cos(x - pi/2)
+      const float f1 = blk ? cos16(r * (c + 1) - 4) : cos16(r * (c + 1));
       const float h0 = round16<TCM>(f0), h1 = round16<TCM>(f1);
       tab[(e * 4 + reg) * 2 + 0] = pack2<TCM>(h0, h1);
       tab[(e * 4 + reg) * 2 + 1] = pack2<TCM>(f0 - h0, f1 - h1);
@@ -107,19 +100,50 @@ __device__ __forceinline__ void build_table(uint32_t* tab, int tid, int nthreads
   }
 }
 
+// x0, x1 rounded to the 16-bit type (hi) and their rounding errors (lo), packed
+template <int TCM>
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+  if constexpr (TCM == kFp16) {
+    const __half2 h = __floats2half2_rn(x0, x1);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(x0 - hf.x, x1 - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  } else {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  }
+}
+
+// D += A_hi B_hi + A_hi B_lo + A_lo B_hi for one 16 x 8 output tile
+template <int TCM>
+__device__ __forceinline__ void mma3(float (&d)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4], uint32_t bh0,
+                                     uint32_t bh1, uint32_t bl0, uint32_t bl1) {
+  mma16816<TCM>(d, ah, bh0, bh1);
+  mma16816<TCM>(d, ah, bl0, bl1);
+  mma16816<TCM>(d, al, bh0, bh1);
+}
+
 // In-place 16-point DFT of every lane's v[0..15] (all 32 lanes must call).
 template <bool INV, int TCM>
 __device__ __forceinline__ void dft16(float2* v, uint32_t* ws, const uint32_t* tab) {
   const int lane = threadIdx.x & 31;
   const int g = lane >> 2, q = lane & 3;
-  // power-of-two scale of this column
-  float m = 0.f;
+  // fp16: power-of-two scale of this column (bf16 has the float exponent range)
+  float s = 1.f, inv_s = 1.f;
+  if constexpr (TCM == kFp16) {
+    float m = 0.f;
 #pragma unroll
-  for (int k = 0; k < 16; ++k) m = fmaxf(m, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
-  // m < 2^e from the biased exponent E of m (E = 0 for zero and subnormal m),
-  // e clamped to [-126, 126] so that both 2^-e and 2^e are normal floats
-  const int e = min(max(((__float_as_int(m) >> 23) & 255) - 126, -126), 126);
-  const float s = __int_as_float((127 - e) << 23), inv_s = __int_as_float((127 + e) << 23);
+    for (int k = 0; k < 16; ++k) m = fmaxf(m, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
+    // m < 2^e from the biased exponent E of m (E = 0 for zero and subnormal m),
+    // e clamped to [-126, 126] so that both 2^-e and 2^e are normal floats
+    const int e = min(max(((__float_as_int(m) >> 23) & 255) - 126, -126), 126);
+    s = __int_as_float((127 - e) << 23);
+    inv_s = __int_as_float((127 + e) << 23);
+  }
   uint32_t* hi = ws;
   uint32_t* lo = ws + 32 * kColWords;
 #pragma unroll
@@ -127,9 +151,7 @@ __device__ __forceinline__ void dft16(float2* v, uint32_t* ws, const uint32_t* t
     const int k0 = (2 * w) & 15, k1 = (2 * w + 1) & 15;
     const float x0 = (w < 8 ? v[k0].x : v[k0].y) * s;
     const float x1 = (w < 8 ? v[k1].x : v[k1].y) * s;
-    const float h0 = round16<TCM>(x0), h1 = round16<TCM>(x1);
-    hi[lane * kColWords + w] = pack2<TCM>(h0, h1);
-    lo[lane * kColWords + w] = pack2<TCM>(x0 - h0, x1 - h1);
+    split2<TCM>(x0, x1, hi[lane * kColWords + w], lo[lane * kColWords + w]);
   }
   __syncwarp();
   float acc[2][4][4];
@@ -139,29 +161,37 @@ __device__ __forceinline__ void dft16(float2* v, uint32_t* ws, const uint32_t* t
     for (int j = 0; j < 4; ++j)
 #pragma unroll
       for (int c = 0; c < 4; ++c) acc[i][j][c] = 0.f;
-  const int dir = INV ? 1 : 0;
+  // A blocks (i, kk): (0,0) and (1,1) are C; (0,1) is -Im W = +S forward, -S inverse;
+  // (1,0) is Im W = -S forward, +S inverse.  Negation flips the sign bits of both halves.
+  uint32_t ch[4], cl[4], sh[4], sl[4], nh[4], nl[4];
+#pragma unroll
+  for (int reg = 0; reg < 4; ++reg) {
+    ch[reg] = tab[(lane * 4 + reg) * 2 + 0];
+    cl[reg] = tab[(lane * 4 + reg) * 2 + 1];
+    sh[reg] = tab[((32 + lane) * 4 + reg) * 2 + 0];
+    sl[reg] = tab[((32 + lane) * 4 + reg) * 2 + 1];
+    nh[reg] = sh[reg] ^ 0x80008000u;
+    nl[reg] = sl[reg] ^ 0x80008000u;
+  }
 #pragma unroll
   for (int kk = 0; kk < 2; ++kk) {
-    uint32_t ah[2][4], al[2][4];
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      const uint32_t* t = tab + ((((dir * 2 + i) * 2 + kk) * 32 + lane) * 4) * 2;
-#pragma unroll
-      for (int reg = 0; reg < 4; ++reg) {
-        ah[i][reg] = t[reg * 2 + 0];
-        al[i][reg] = t[reg * 2 + 1];
-      }
-    }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int n = 8 * j + g;
       const uint32_t bh0 = hi[n * kColWords + 8 * kk + q], bh1 = hi[n * kColWords + 8 * kk + q + 4];
       const uint32_t bl0 = lo[n * kColWords + 8 * kk + q], bl1 = lo[n * kColWords + 8 * kk + q + 4];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        mma16816<TCM>(acc[i][j], ah[i], bh0, bh1);
-        mma16816<TCM>(acc[i][j], ah[i], bl0, bl1);
-        mma16816<TCM>(acc[i][j], al[i], bh0, bh1);
+      if (kk == 0) {
+        mma3<TCM>(acc[0][j], ch, cl, bh0, bh1, bl0, bl1);
+        if (INV)
+          mma3<TCM>(acc[1][j], sh, sl, bh0, bh1, bl0, bl1);
+        else
+          mma3<TCM>(acc[1][j], nh, nl, bh0, bh1, bl0, bl1);
+      } else {
+        if (INV)
+          mma3<TCM>(acc[0][j], nh, nl, bh0, bh1, bl0, bl1);
+        else
+          mma3<TCM>(acc[0][j], sh, sl, bh0, bh1, bl0, bl1);
+        mma3<TCM>(acc[1][j], ch, cl, bh0, bh1, bl0, bl1);
       }
     }
   }
