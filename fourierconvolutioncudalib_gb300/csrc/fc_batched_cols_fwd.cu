@@ -8,7 +8,7 @@
 
 namespace fc {
 namespace fast {
-FC_DEFINE_BATCH_KERNEL(k_batch_cols_fwd, 2, FC_COL_SIZES, col_fwd_task, , )
+FC_DEFINE_BATCH_KERNEL(k_batch_cols_fwd, 2, FC_BATCH_COL_SIZES, col_fwd_task, , )
 }  // namespace fast
 
 long long batched_col_tiles(int n, int ncols, long long planes) {
@@ -16,7 +16,7 @@ long long batched_col_tiles(int n, int ncols, long long planes) {
 #define FC_CASE(n_) \
   case n_:          \
     return (long long)((ncols + fast::ColGeom<n_>::B - 1) / fast::ColGeom<n_>::B) * planes;
-    FC_COL_SIZES(FC_CASE)
+    FC_BATCH_COL_SIZES(FC_CASE)
 #undef FC_CASE
     default:
       return 0;
@@ -29,7 +29,7 @@ size_t batched_col_smem(int n, bool zconv) {
 #define FC_CASE(n_) \
   case n_:          \
     return sizeof(float2) * fast::ColGeom<n_>::SMEM;
-    FC_COL_SIZES(FC_CASE)
+    FC_BATCH_COL_SIZES(FC_CASE)
 #undef FC_CASE
     default:
       return 0;

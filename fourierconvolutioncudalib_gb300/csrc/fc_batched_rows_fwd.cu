@@ -8,7 +8,7 @@
 
 namespace fc {
 namespace fast {
-FC_DEFINE_BATCH_KERNEL(k_batch_rows_fwd, 2, FC_ROW_SIZES, row_fwd_task, , )
+FC_DEFINE_BATCH_KERNEL(k_batch_rows_fwd, 2, FC_BATCH_ROW_SIZES, row_fwd_task, , )
 }  // namespace fast
 
 long long batched_row_tiles(int n, long long rows) {
@@ -16,7 +16,7 @@ long long batched_row_tiles(int n, long long rows) {
 #define FC_CASE(n_) \
   case n_:          \
     return fast::RowGeom<n_>::tiles(rows);
-    FC_ROW_SIZES(FC_CASE)
+    FC_BATCH_ROW_SIZES(FC_CASE)
 #undef FC_CASE
     default:
       return 0;
@@ -28,7 +28,7 @@ size_t batched_row_smem(int n) {
 #define FC_CASE(n_) \
   case n_:          \
     return sizeof(float2) * fast::RowGeom<n_>::SMEM;
-    FC_ROW_SIZES(FC_CASE)
+    FC_BATCH_ROW_SIZES(FC_CASE)
 #undef FC_CASE
     default:
       return 0;

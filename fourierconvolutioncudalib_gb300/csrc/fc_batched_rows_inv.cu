@@ -8,7 +8,7 @@
 
 namespace fc {
 namespace fast {
-FC_DEFINE_BATCH_KERNEL(k_batch_rows_inv, 2, FC_ROW_SIZES, row_inv_task, , )
+FC_DEFINE_BATCH_KERNEL(k_batch_rows_inv, 2, FC_BATCH_ROW_SIZES, row_inv_task, , )
 }  // namespace fast
 
 cudaError_t batched_rows_inv(const BTask* tasks, int ntasks, long long total_tiles, int grid, size_t smem,

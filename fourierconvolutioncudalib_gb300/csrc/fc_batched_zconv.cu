@@ -10,7 +10,7 @@
 
 namespace fc {
 namespace fast {
-FC_DEFINE_BATCH_KERNEL(k_batch_zconv, 1, FC_COL_SIZES, z_task, FC_COMMA int stash_off, )
+FC_DEFINE_BATCH_KERNEL(k_batch_zconv, 1, FC_BATCH_COL_SIZES, z_task, FC_COMMA int stash_off, )
 }  // namespace fast
 
 cudaError_t batched_zconv(const BTask* tasks, int ntasks, long long total_tiles, int grid, size_t smem,

@@ -1373,8 +1373,9 @@ static void enqueue_batched(DevCtx& c, int nv, const float* const* imgs, float* 
       e->g.push_back(g);
       e->off.push_back(off);
       const Axes a = axes_for(c, g);  // twiddles exist before any capture
-      const bool fast = !compat && use_fast() && fast_rows_supported(g.nx) && fast_cols_supported(g.ny) &&
-                        fast_cols_supported(g.nz);
+      // lengths the persistent batched kernels cover (a subset of the single-volume ones)
+      const bool fast = !compat && use_fast() && batched_row_tiles(g.nx, 1) > 0 && batched_col_tiles(g.ny, 1, 1) > 0 &&
+                        batched_col_tiles(g.nz, 1, 1) > 0;
       if (fast) {
         size_t before[5];
         for (int p = 0; p < 5; ++p) before[p] = e->tasks[p].size();

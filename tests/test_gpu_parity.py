@@ -98,6 +98,10 @@ def test_c1_vs_cufft_sequence(cuda, orc, kernels):
     ((160, 288, 320), (21, 25, 23)),  # batch-view lengths: radices 10 and 9
     ((64, 352, 400), (9, 11, 13)),    # radices 11 and 5
     ((200, 96, 224), (7, 5, 9)),      # radix 10 chain along z, 14 along x
+    ((100, 500, 500), (21, 15, 15)),  # common stack extents: 10x10, 10x10x5
+    ((60, 120, 1000), (9, 7, 5)),     # 1000 rows (10x10x10), 12x10 columns, 15x4 along z
+    ((150, 360, 72), (11, 9, 7)),     # 15x10 along z, 15x12x2 columns, 12x6 rows
+    ((24, 900, 20), (5, 7, 3)),       # 15x15x4 columns, short rows of 20
 ])
 def test_shapes_vs_fp64(cuda, orc, kernels, host_io, shape, kshape):
     rng = np.random.default_rng(sum(shape) + sum(kshape))
