@@ -124,7 +124,7 @@ struct DevCtx {
   std::map<int, float2*> twiddles;  // per transform length
   // side stream and events of the kernel-spectrum fork (created on first use)
   cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_aux = nullptr, ev_done = nullptr;
   // streams and events of the view-concurrent batched schedule (created on first use)
   std::vector<cudaStream_t> bstreams;
   std::vector<cudaEvent_t> bevents;
@@ -135,7 +135,7 @@ struct DevCtx {
 // fused z pass waits for them.
 struct Fork {
   cudaStream_t side;
-  cudaEvent_t forked, joined;
+  cudaEvent_t forked, joined, aux, done;
 };
 
 static std::mutex g_ctx_mu;
@@ -364,12 +364,21 @@ static bool tc_len(int n) { return n == 128 || n == 256 || n == 512 || n == 1024
 
 // Pipelined x passes (fc_fast_pipe.cu); FC_PIPE=0 selects the one-tile-per-CTA kernels.
 static int g_pipe = -1;
+// set while the enqueue in progress on this thread targets a stream that runs
+// beside a persistent pass (whose CTAs take a static share of the tiles and
+// should not have to wait for SMs held by this stream's work)
+static thread_local bool t_no_pipe = false;
+struct NoPipeScope {
+  bool prev;
+  NoPipeScope() : prev(t_no_pipe) { t_no_pipe = true; }
+  ~NoPipeScope() { t_no_pipe = prev; }
+};
 static bool use_pipe() {
   if (g_pipe < 0) {
     const char* e = std::getenv("FC_PIPE");
     g_pipe = e ? std::atoi(e) : 1;
   }
-  return g_pipe != 0;
+  return g_pipe != 0 && !t_no_pipe;
 }
 // in-place y passes on wide tiles (FC_COLS_WIDE=0: the 256-thread tiles)
 static int g_cols_wide = -1;
@@ -578,8 +587,10 @@ static Fork ctx_fork(DevCtx& c) {
     cuda_check(cudaStreamCreateWithPriority(&c.side, cudaStreamNonBlocking, hi), "cudaStreamCreate(side)");
     cuda_check(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
     cuda_check(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaEventCreateWithFlags(&c.ev_aux, cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaEventCreateWithFlags(&c.ev_done, cudaEventDisableTiming), "cudaEventCreate");
   }
-  return Fork{c.side, c.ev_fork, c.ev_join};
+  return Fork{c.side, c.ev_fork, c.ev_join, c.ev_aux, c.ev_done};
 }
 
 static void enqueue_conv(DevCtx& c, const Geom& g0, const float* d_image, float* d_out, const float* d_kernel,
@@ -684,34 +695,60 @@ static void enqueue_adjoint(DevCtx& c, const Geom& g, const float* d_x, const fl
   float* GKR = (float*)(ws + L.off_GKR);
   const float scale = 1.0f / (float)g.N();
   const int hz = g.kbox ? g.kz / 2 : 0;
-  enqueue_xy_fwd(g, a, t, d_g, SG, st, "grad_x_r2c", "grad_y_fwd");
-  if (d_gk) {
-    enqueue_xy_fwd(g, a, t, d_x, SX, st, "image_x_r2c", "image_y_fwd");
-    FC_PASS("zcorr_crop", 16.0 * g.nxh * (double)g.ny * g.nz + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
-            d_zcorr(SX, SG, GK, g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, a.z, t.z_cols_log2, t.threads,
-                              st));
+  // The kernel spectrum and the kernel-gradient tail run on the side stream:
+  // the spectrum from after the gradient's x pass until the fused z pass
+  // needs it, the tail once the correlation has produced GK.
+  const bool split = use_fork();
+  Fork f{};
+  if (split) f = ctx_fork(c);
+  const cudaStream_t ks = split ? f.side : st;
+  const long long rows_all = (long long)g.ny * g.nz;
+  FC_PASS("grad_x_r2c", 4.0 * g.N() + 8.0 * g.nxh * rows_all, st,
+          d_x_r2c_dense(d_g, g.nx, SG, g.pitch, rows_all, a.x, t, st));
+  if (split) {
+    cuda_check(cudaEventRecord(f.forked, st), "cudaEventRecord(fork)");
+    cuda_check(cudaStreamWaitEvent(f.side, f.forked, 0), "cudaStreamWaitEvent(fork)");
   }
   if (d_gx) {
     Layout kl;
     kl.off_KX = L.off_KX;
     kl.off_KXY = L.off_KXY;
-    enqueue_kernel_spectrum(g, a, t, d_k, ws, kl, st);
+    enqueue_kernel_spectrum(g, a, t, d_k, ws, kl, ks);
+    if (split) cuda_check(cudaEventRecord(f.joined, ks), "cudaEventRecord(join)");
+  }
+  FC_PASS("grad_y_fwd", 16.0 * g.nxh * rows_all, st,
+          d_cols(SG, SG, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2, t.threads, st));
+  if (d_gk) {
+    enqueue_xy_fwd(g, a, t, d_x, SX, st, "image_x_r2c", "image_y_fwd");
+    FC_PASS("zcorr_crop", 16.0 * g.nxh * (double)g.ny * g.nz + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
+            d_zcorr(SX, SG, GK, g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, a.z, t.z_cols_log2, t.threads,
+                              st));
+    if (split) {
+      cuda_check(cudaEventRecord(f.aux, st), "cudaEventRecord");
+      cuda_check(cudaStreamWaitEvent(ks, f.aux, 0), "cudaStreamWaitEvent");
+    }
+    NoPipeScope np;
+    const long long rows = (long long)g.ny * g.kplanes;
+    FC_PASS("grad_kernel_y_inv", 16.0 * g.nxh * rows, ks,
+            d_cols(GK, GK, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.kplanes, true, a.y, t.y_cols_log2,
+                        t.threads, ks));
+    float* dst = g.kbox ? GKR : d_gk;
+    FC_PASS("grad_kernel_x_c2r", 8.0 * g.nxh * rows + 4.0 * g.nx * rows, ks,
+            d_x_c2r(GK, g.pitch, dst, g.nx, rows, a.x, t, ks));
+    if (g.kbox)
+      FC_PASS("grad_kernel_crop", 8.0 * g.kx * g.ky * g.kz, ks,
+              launch_crop_kernel(GKR, g.nx, g.ny, g.nx, g.kx, g.ky, g.kz, d_gk, ks));
+  }
+  if (d_gx) {
+    if (split) cuda_check(cudaStreamWaitEvent(st, f.joined, 0), "cudaStreamWaitEvent(join)");
     FC_PASS("zconv_conj", 16.0 * g.nxh * (double)g.ny * g.nz + 8.0 * g.nxh * (double)g.ny * g.kplanes, st,
             d_zconv(SG, (const float2*)(ws + L.off_KXY), g.pitch, g.ny, g.nxh, g.kplanes, hz, scale, true, a.z,
                          t.z_cols_log2, t.threads, st));
     enqueue_yx_inv(g, a, t, SG, d_gx, st, "grad_image_y_inv", "grad_image_x_c2r");
   }
-  if (d_gk) {
-    const long long rows = (long long)g.ny * g.kplanes;
-    FC_PASS("grad_kernel_y_inv", 16.0 * g.nxh * rows, st,
-            d_cols(GK, GK, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.kplanes, true, a.y, t.y_cols_log2,
-                        t.threads, st));
-    float* dst = g.kbox ? GKR : d_gk;
-    FC_PASS("grad_kernel_x_c2r", 8.0 * g.nxh * rows + 4.0 * g.nx * rows, st,
-            d_x_c2r(GK, g.pitch, dst, g.nx, rows, a.x, t, st));
-    if (g.kbox)
-      FC_PASS("grad_kernel_crop", 8.0 * g.kx * g.ky * g.kz, st,
-              launch_crop_kernel(GKR, g.nx, g.ny, g.nx, g.kx, g.ky, g.kz, d_gk, st));
+  if (split) {
+    cuda_check(cudaEventRecord(f.done, ks), "cudaEventRecord");
+    cuda_check(cudaStreamWaitEvent(st, f.done, 0), "cudaStreamWaitEvent");
   }
 }
 
@@ -1693,6 +1730,8 @@ int fc_release_device(int devCUDA) {
     if (c->side) cudaStreamDestroy(c->side);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_aux) cudaEventDestroy(c->ev_aux);
+    if (c->ev_done) cudaEventDestroy(c->ev_done);
     for (cudaStream_t s2 : c->bstreams) cudaStreamDestroy(s2);
     for (cudaEvent_t e2 : c->bevents) cudaEventDestroy(e2);
     cudaSetDevice(prev);
