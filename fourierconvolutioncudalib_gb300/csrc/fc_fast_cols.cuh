@@ -98,10 +98,13 @@ template <int N>
 using ZTile = ColGeomB<N, 16>;
 template <int N>
 struct ZGeom {
-  // exchange tile, stash, image stage buffer (float2 elements)
+  // exchange tile, stash, image stage buffer (float2 elements); the stash
+  // starts on a 16-byte boundary (the exchange tile has N*B + N*B/16 entries,
+  // odd for some lengths) so that the stage buffer after it, the target of
+  // 16-byte cp.async copies, is 16-byte aligned too
+  static constexpr int XCH = (ZTile<N>::SMEM + 1) & ~1;
   static constexpr int STAGE = N * ZTile<N>::B;
-  static constexpr int SMEM_BYTES =
-      (ZTile<N>::SMEM + ZTile<N>::THREADS * kVals + STAGE) * (int)sizeof(float2);
+  static constexpr int SMEM_BYTES = (XCH + ZTile<N>::THREADS * kVals + STAGE) * (int)sizeof(float2);
   // resident CTAs requested from the register allocator (256 threads: 2 -> <= 128 registers)
   static constexpr int MIN_BLOCKS =
       ZTile<N>::THREADS <= 256 ? FC_ZCONV_MIN_BLOCKS * (256 / ZTile<N>::THREADS) : 1;
@@ -184,8 +187,8 @@ __global__ void __launch_bounds__(ZTile<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zco
     float scale, const float2* __restrict__ W) {
   using G = ZTile<N>;
   extern __shared__ __align__(16) float2 zsm[];
-  float2* stash = zsm + G::SMEM;
-  float2* stage = stash + G::THREADS * kVals;
+  float2* stash = zsm + ZGeom<N>::XCH;
+  float2* stage = stash + G::THREADS * kVals;  // THREADS * kVals is even: 16-byte aligned
   body_zconv<N, CONJ, tc::kNone, G>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, W, (int)blockIdx.x,
                                     (int)blockIdx.y, (int)threadIdx.x, zsm, stash, G::THREADS,
                                     TcCtx{nullptr, nullptr}, stage);

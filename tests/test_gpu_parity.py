@@ -102,6 +102,9 @@ def test_c1_vs_cufft_sequence(cuda, orc, kernels):
     ((60, 120, 1000), (9, 7, 5)),     # 1000 rows (10x10x10), 12x10 columns, 15x4 along z
     ((150, 360, 72), (11, 9, 7)),     # 15x10 along z, 15x12x2 columns, 12x6 rows
     ((24, 900, 20), (5, 7, 3)),       # 15x15x4 columns, short rows of 20
+    ((250, 48, 64), (9, 5, 7)),       # z lengths whose fused-z tiles are 8 and 4 columns wide
+    ((500, 20, 30), (7, 3, 5)),
+    ((900, 24, 20), (11, 5, 3)),
 ])
 def test_shapes_vs_fp64(cuda, orc, kernels, host_io, shape, kshape):
     rng = np.random.default_rng(sum(shape) + sum(kshape))
