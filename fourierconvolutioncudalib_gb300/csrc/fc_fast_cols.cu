@@ -98,27 +98,47 @@ cudaError_t fast_cols(const float2* src, float2* dst, long long ps, long long es
 }
 
 namespace fast {
+template <int N, bool INV, class Src>
+static cudaError_t launch_cols_wide(Src src, float2* dst, long long ps, long long es, int ncols, int nplanes,
+                                   const float2* W, cudaStream_t st) {
+  using G = ColGeomWide<N>;
+  constexpr int sm = G::SMEM * (int)sizeof(float2);
+  if (sm > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_cols_wide<N, INV, Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess) return e;
+  }
+  const dim3 grid((ncols + G::B - 1) / G::B, nplanes);
+  k_cols_wide<N, INV, Src><<<grid, G::THREADS, sm, st>>>(src, dst, ps, es, ncols, W);
+  return cudaGetLastError();
+}
+
 template <int N, bool INV>
 static cudaError_t run_cols_wide(float2* S, long long ps, long long es, int ncols, int nplanes, const float2* W,
                                  cudaStream_t st) {
   using G = ColGeomWide<N>;
   // measured on GB300: wider tiles pay off for columns of 1024 (32-byte row
-  // segments otherwise) and cost time at 512 and below
-  if constexpr (G::B == ColGeom<N>::B || N < 1024) {
+  // segments otherwise) and cost time at 512 and below; 2048 has only the
+  // wide kernel (the 256-thread tile would not fit static shared memory)
+  if constexpr ((G::B == ColGeom<N>::B || N < 1024) && N <= 1024) {
     return run_cols<N, INV, ColPlain>(ColPlain{S, ps, es}, S, ps, es, ncols, nplanes, W, st);
   } else {
-    constexpr int sm = G::SMEM * (int)sizeof(float2);
-    if (sm > 48 * 1024) {
-      const cudaError_t e =
-          cudaFuncSetAttribute(k_cols_wide<N, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-      if (e != cudaSuccess) return e;
-    }
-    const dim3 grid((ncols + G::B - 1) / G::B, nplanes);
-    k_cols_wide<N, INV><<<grid, G::THREADS, sm, st>>>(S, ps, es, ncols, W);
-    return cudaGetLastError();
+    return launch_cols_wide<N, INV, ColPlain>(ColPlain{S, ps, es}, S, ps, es, ncols, nplanes, W, st);
   }
 }
 }  // namespace fast
+
+bool fast_cols_wide_supported(int n) {
+  switch (n) {
+#define FC_CASE(n_) case n_:
+    FC_COL_SIZES(FC_CASE)
+    FC_WIDE_ONLY_SIZES(FC_CASE)
+#undef FC_CASE
+    return true;
+    default:
+      return false;
+  }
+}
 
 cudaError_t fast_cols_wide(float2* S, long long ps, long long es, int ncols, int nplanes, bool inverse,
                            const FcAxis& ax, cudaStream_t st) {
@@ -129,6 +149,22 @@ cudaError_t fast_cols_wide(float2* S, long long ps, long long es, int ncols, int
     return inverse ? fast::run_cols_wide<n_, true>(S, ps, es, ncols, nplanes, ax.W, st)  \
                    : fast::run_cols_wide<n_, false>(S, ps, es, ncols, nplanes, ax.W, st);
     FC_COL_SIZES(FC_CASE)
+    FC_WIDE_ONLY_SIZES(FC_CASE)
+#undef FC_CASE
+    default:
+      return cudaErrorNotSupported;
+  }
+}
+
+cudaError_t fast_cols_kx_wide(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
+                              int nplanes, const FcAxis& ax, cudaStream_t st) {
+  if (nplanes <= 0 || ncols <= 0) return cudaSuccess;
+  const ColKX s{kx_spec, pitch, krows, hy, ax.n};
+  switch (ax.n) {
+#define FC_CASE(n_) \
+  case n_:          \
+    return fast::launch_cols_wide<n_, false, ColKX>(s, dst, (long long)ax.n * pitch, pitch, ncols, nplanes, ax.W, st);
+    FC_WIDE_ONLY_SIZES(FC_CASE)
 #undef FC_CASE
     default:
       return cudaErrorNotSupported;

@@ -69,12 +69,12 @@ __device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long
 }
 
 // y pass on wide tiles (dynamic shared memory of ColGeomWide<N>::SMEM float2)
-template <int N, bool INV>
-__global__ void __launch_bounds__(ColGeomWide<N>::THREADS, 1024 / ColGeomWide<N>::THREADS) k_cols_wide(float2* S, long long ps, long long es,
-                                                                       int ncols, const float2* __restrict__ W) {
+template <int N, bool INV, class Src>
+__global__ void __launch_bounds__(ColGeomWide<N>::THREADS, 1024 / ColGeomWide<N>::THREADS)
+    k_cols_wide(Src src, float2* dst, long long ps, long long es, int ncols, const float2* __restrict__ W) {
   extern __shared__ __align__(16) float2 wsm[];
-  body_cols<N, INV, ColPlain, tc::kNone, ColGeomWide<N>>(ColPlain{S, ps, es}, S, ps, es, ncols, W, (int)blockIdx.x,
-                                                         (int)blockIdx.y, (int)threadIdx.x, wsm);
+  body_cols<N, INV, Src, tc::kNone, ColGeomWide<N>>(src, dst, ps, es, ncols, W, (int)blockIdx.x, (int)blockIdx.y,
+                                                    (int)threadIdx.x, wsm);
 }
 
 template <int N, bool INV, class Src>

@@ -15,3 +15,6 @@
 #define FC_BATCH_COL_SIZES(X) FC_FAST_COMMON_SIZES(X)
 #define FC_ROW_SIZES(X) FC_BATCH_ROW_SIZES(X) FC_EXTRA_SIZES(X)
 #define FC_COL_SIZES(X) FC_BATCH_COL_SIZES(X) FC_EXTRA_SIZES(X)
+// column lengths served only by the wide in-place y pass (its exchange tile
+// needs dynamic shared memory): 2048-row camera frames
+#define FC_WIDE_ONLY_SIZES(X) X(2048)

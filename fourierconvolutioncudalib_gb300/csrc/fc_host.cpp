@@ -430,6 +430,8 @@ static cudaError_t d_cols(const float2* src, float2* dst, long long ps, long lon
     if (src == dst && cols_wide()) return fast_cols_wide(dst, ps, es, ncols, nplanes, inv, ax, st);
     return fast_cols(src, dst, ps, es, ncols, nplanes, inv, ax, st);
   }
+  if (use_fast() && src == dst && fast_cols_wide_supported(ax.n))
+    return fast_cols_wide(dst, ps, es, ncols, nplanes, inv, ax, st);
   return launch_cols(src, dst, ps, es, ncols, nplanes, inv, ax, cols_log2, threads, st);
 }
 static cudaError_t d_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
@@ -438,6 +440,8 @@ static cudaError_t d_cols_kx(const float2* kx_spec, long long pitch, int krows, 
     return FC_TC_CALL(tc_cols, 2, kx_spec, pitch, krows, hy, dst, (long long)ax.n * pitch, pitch, ncols, nplanes, ax,
                       st);
   if (use_fast() && fast_cols_supported(ax.n)) return fast_cols_kx(kx_spec, pitch, krows, hy, dst, ncols, nplanes, ax, st);
+  if (use_fast() && fast_cols_wide_supported(ax.n))
+    return fast_cols_kx_wide(kx_spec, pitch, krows, hy, dst, ncols, nplanes, ax, st);
   return launch_cols_kx(kx_spec, pitch, krows, hy, dst, ncols, nplanes, ax, cols_log2, threads, st);
 }
 static cudaError_t d_zconv(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,

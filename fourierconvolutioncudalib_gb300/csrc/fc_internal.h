@@ -107,7 +107,12 @@ cudaError_t pipe_x_r2c_dense(const float* in, long long in_pitch, float2* out, l
 cudaError_t pipe_x_c2r(const float2* in, long long in_pitch, float* out, long long out_pitch, long long nrows,
                        const FcAxis& ax, cudaStream_t st);
 unsigned int pipe_take_timeouts();
-// in-place y pass on wide tiles (fast::ColGeomWide)
+// in-place y pass on wide tiles (fast::ColGeomWide); covers the column
+// lengths plus FC_WIDE_ONLY_SIZES
+bool fast_cols_wide_supported(int n);
+// kernel y pass on wide tiles for the FC_WIDE_ONLY_SIZES lengths
+cudaError_t fast_cols_kx_wide(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,
+                              int nplanes, const FcAxis& ax, cudaStream_t st);
 cudaError_t fast_cols_wide(float2* S, long long ps, long long es, int ncols, int nplanes, bool inverse,
                            const FcAxis& ax, cudaStream_t st);
 cudaError_t fast_cols_kx(const float2* kx_spec, long long pitch, int krows, int hy, float2* dst, int ncols,

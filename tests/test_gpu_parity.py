@@ -92,7 +92,7 @@ def test_c1_vs_cufft_sequence(cuda, orc, kernels):
     ((37, 79, 109), (5, 5, 5)),       # large primes from the padded reference KAT extents
     ((128, 512, 512), (63, 31, 31)),  # the microscope configuration's shapes
     ((64, 256, 1024), (9, 9, 9)),     # 1024 rows
-    ((16, 2048, 128), (3, 5, 3)),     # a 2048 column axis (generic kernels)
+    ((16, 2048, 128), (3, 5, 3)),     # a 2048 column axis (wide y tiles; generic kernel y pass)
     ((256, 64, 32), (5, 3, 3)),       # short rows, long z
     ((96, 448, 384), (63, 31, 31)),   # the non-power-of-two microscope configuration (radices 16, 14, 12, 6, 2)
     ((160, 288, 320), (21, 25, 23)),  # batch-view lengths: radices 10 and 9
