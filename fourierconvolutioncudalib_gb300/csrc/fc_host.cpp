@@ -1019,7 +1019,8 @@ struct BatchEntry {
   int choice[5] = {kFatOcc, kFatOcc, kFatOcc, kFatOcc, kFatOcc};
   // 0: pass-major (one launch per pass over all views); 1: view-major (each
   // view's passes in turn, its spectra stay in L2); 2: view-concurrent (the
-  // views' pass chains on kBatchStreams streams, parallel graph branches)
+  // views' pass chains on kBatchStreams streams, parallel graph branches);
+  // 3: the single-volume pass sequence per view (kernel spectrum forked)
   int schedule = 0;
   std::vector<std::vector<std::pair<int, int>>> view_tasks;  // per fast view: (pass, task index)
   cudaGraph_t graph = nullptr;
@@ -1225,6 +1226,11 @@ static void run_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, float*
   if (E.schedule == 1) {
     for (const auto& vt : E.view_tasks)
       for (const auto& pt : vt) launch_task(E.tasks[pt.first][pt.second], pt.first, st, true);
+  } else if (E.schedule == 3) {
+    for (size_t v = 0; v < E.g.size(); ++v)
+      if (std::find(E.slow_views.begin(), E.slow_views.end(), (int)v) == E.slow_views.end())
+        enqueue_conv(c, E.g[v], imgs[v], outs[v], kers[v], false, ws + E.off[v], plain_layout(E.g[v], false).total,
+                     st);
   } else if (E.schedule == 2) {
     const int P = kBatchStreams;
     while ((int)c.bstreams.size() < P) {
@@ -1283,7 +1289,7 @@ static bool tune_lookup(const std::string& sig, int* choice, int* schedule) {
     for (int i = 0; i < 6; ++i) ok = ok && (bool)(is >> ch[i]);
     if (!ok) continue;
     for (int i = 0; i < 5; ++i) choice[i] = ch[i];
-    if (ch[5] < 0 || ch[5] > 2) continue;
+    if (ch[5] < 0 || ch[5] > 3) continue;
     *schedule = ch[5];
     return true;
   }
@@ -1349,9 +1355,9 @@ static void autotune_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, f
     E.choice[p] = best_choice;
   }
   // whole batch: the tuned pass-major schedule against the view-major and view-concurrent ones
-  static const char* const kSchedName[3] = {"pass-major", "view-major", "view-concurrent"};
-  float t_sched[3] = {1e30f, 1e30f, 1e30f};
-  for (int sc = 0; sc < 3; ++sc) {
+  static const char* const kSchedName[4] = {"pass-major", "view-major", "view-concurrent", "plain-per-view"};
+  float t_sched[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+  for (int sc = 0; sc < 4; ++sc) {
     E.schedule = sc;
     for (int r = 0; r < 4; ++r) {
       cuda_check(cudaEventRecord(a, st), "cudaEventRecord");
@@ -1365,7 +1371,7 @@ static void autotune_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, f
     if (tune_log()) std::fprintf(stderr, "fc tune schedule %s: %.1f us\n", kSchedName[sc], 1e3 * t_sched[sc]);
   }
   E.schedule = 0;
-  for (int sc = 1; sc < 3; ++sc)
+  for (int sc = 1; sc < 4; ++sc)
     if (t_sched[sc] < t_sched[E.schedule]) E.schedule = sc;
   cudaEventDestroy(a);
   cudaEventDestroy(b);

@@ -232,7 +232,7 @@ def profile(enable: Optional[bool] = None, only: Optional[str] = None) -> List[T
         L.fc_profile_only((only or "").encode())
         L.fc_profile_enable(1 if enable else 0)
         return []
-    cap = 4096
+    cap = 1 << 16
     names = ctypes.create_string_buffer(64 * cap)
     ms = (ctypes.c_float * cap)()
     by = (ctypes.c_double * cap)()
