@@ -208,8 +208,10 @@ def run_ours(args, cfg, world, rank, local):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
 
+    tc_flag = {"fp16": fc.FC_FLAG_TC_FP16, "bf16": fc.FC_FLAG_TC_BF16}.get(args.tc, 0)
+
     def step():
-        fcd.conv3d(img, ker, out=out, workspace=ws)
+        fcd.conv3d(img, ker, out=out, workspace=ws, flags=tc_flag)
 
     for _ in range(args.warmup):
         flush.zero_()
@@ -281,7 +283,8 @@ def run_ours(args, cfg, world, rank, local):
     tf = ROOT / "profiles" / "ncu_traffic.json"
     if dom and tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get(cfg["workload"], {}).get(dom["pass"])
+            wl = cfg["workload"] + (f"_tc_{args.tc}" if tc_flag else "")
+            traffic = json.loads(tf.read_text()).get(wl, {}).get(dom["pass"])
         except Exception:
             traffic = None
     Mc = (nx // 2 + 1) * ny * nz
@@ -362,8 +365,10 @@ def run_ours(args, cfg, world, rank, local):
         line = {
             "metric": METRIC, "value": value, "unit": "Gvoxel/s", "n_gpus": world, "steps": K,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, configuration shapes and distribution)",
-            "config": {"workload": cfg["workload"], "image_xyz": [nx, ny, nz], "kernel_xyz": [kx, ky, kz],
+            "vs_baseline": None, "dtype": "f32" if not tc_flag else f"f32 data, {args.tc} hi+lo tensor-core DFT stages",
+            "data": "synthetic (seeded, configuration shapes and distribution)",
+            "config": {"workload": cfg["workload"] + (f"_tc_{args.tc}" if tc_flag else ""), "image_xyz": [nx, ny, nz],
+                       "kernel_xyz": [kx, ky, kz],
                        "api": "fc_conv3d_device", "l2": "flushed before every step (256 MiB write outside the "
                                                          "step events)", "parallelism": f"replicas x{world}"},
             "wall_s_timed_region": t1 - t0,
@@ -622,6 +627,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ref-cufft", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
+    ap.add_argument("--tc", choices=["fp16", "bf16"], default=None,
+                    help="time the tensor-core precision mode instead of the fp32 path")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
