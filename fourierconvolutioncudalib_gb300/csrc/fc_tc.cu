@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS) k_r2c_tc(Src src, float2*
 }
 
 template <int N>
-__global__ void __launch_bounds__(RowGeom<N>::THREADS) k_c2r_tc(const float2* __restrict__ in, long long in_pitch,
+__global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_c2r_tc(const float2* __restrict__ in, long long in_pitch,
                                                                 float* __restrict__ out, long long out_pitch,
                                                                 long long nrows, const float2* __restrict__ W) {
   extern __shared__ float2 dsm[];
@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS) k_c2r_tc(const float2* __
 }
 
 template <int N, bool INV, class Src>
-__global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols_tc(Src src, float2* dst, long long ps, long long es,
+__global__ void __launch_bounds__(ColGeom<N>::THREADS, 3) k_cols_tc(Src src, float2* dst, long long ps, long long es,
                                                                  int ncols, const float2* __restrict__ W) {
   extern __shared__ float2 dsm[];
   const TcCtx tcx = tc_setup(dsm + ColGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
