@@ -27,6 +27,7 @@ its sources are not on the GPU host).
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -459,7 +460,13 @@ def time_forms(dev, fcd, torch):
     """Adjoint form on the differentiation configuration (256^3, 21^3) and the
     batched form on the multi-view configuration (6 uneven views), each
     against the plain path on the same GPU, with its error against FP64."""
+    import tempfile
+
     from fourierconvolutioncudalib_gb300 import workloads as W
+
+    # the batched form tunes its launch choices on its first (untimed) call; a
+    # fresh cache file makes it tune against the kernels of this build
+    os.environ.setdefault("FC_TUNE_CACHE", os.path.join(tempfile.mkdtemp(prefix="fc_tune_"), "tune.txt"))
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     out = {}
@@ -509,10 +516,18 @@ def time_forms(dev, fcd, torch):
     fcd.conv3d_batched(imgs, kers, outs=outs, workspace=ws)
     torch.cuda.synchronize()
     errs = [_rel64(o.cpu().numpy(), _fp64_conv(v["image"], v["kernel"])[0]) for o, v in zip(outs, views)]
+    ch = (ctypes.c_int * 5)()
+    sched = fcd.lib().fc_batched_last_plan(ch)
+    sched_names = ["pass-major", "view-major", "view-concurrent", "single-volume sequence per view",
+                   "single-volume sequences concurrently"]
+    choice_names = ["persistent work-list launch", "persistent, one CTA per SM", "one launch per view"]
     out["batched"] = {"workload": "batched_6_views_87M_voxels", "value": nvox / (ms_b / 1e3) / 1e9,
                       "unit": "Gvoxel/s", "ms": ms_b, "sequential_plain_ms": ms_s, "vs_sequential_plain": ms_s / ms_b,
                       "fp64_rel_l2_max_over_views": max(errs),
-                      "how": "one persistent launch per pass over a device work-list, CUDA graph replay"}
+                      "tuned_schedule": sched_names[sched] if 0 <= sched < 5 else None,
+                      "tuned_pass_choices": [choice_names[c] if 0 <= c < 3 else None for c in ch],
+                      "how": "one call; the tuner times persistent work-list launches per pass against per-view "
+                             "launches and five schedules, caches the choice, and the call replays a CUDA graph"}
     # tensor-core precision mode: timing at 1024x1024x256 (63^3 PSF) against the fp32 path,
     # FP64 error at 512x512x128 where every axis has radix-16 stages on the tensor cores
     import fourierconvolutioncudalib_gb300 as fc

@@ -99,6 +99,7 @@ _SIGNATURES = {
     "fc_pad_shift_kernel_device": (_I, [_P, _IP, _IP, _I, _P, _P]),
     "fc_plan_radices": (_I, [_I, _IP, _I]),
     "fc_profile_enable": (None, [_I]),
+    "fc_batched_last_plan": (_I, [_IP]),
     "fc_profile_only": (None, [ctypes.c_char_p]),
     "fc_profile_read": (_I, [ctypes.c_char_p, _I, _FP, ctypes.POINTER(ctypes.c_double), _I]),
     "fc_launch_count": (_I, []),

@@ -1020,7 +1020,8 @@ struct BatchEntry {
   // 0: pass-major (one launch per pass over all views); 1: view-major (each
   // view's passes in turn, its spectra stay in L2); 2: view-concurrent (the
   // views' pass chains on kBatchStreams streams, parallel graph branches);
-  // 3: the single-volume pass sequence per view (kernel spectrum forked)
+  // 3: the single-volume pass sequence per view (kernel spectrum forked);
+  // 4: those sequences on kBatchStreams streams (parallel graph branches)
   int schedule = 0;
   std::vector<std::vector<std::pair<int, int>>> view_tasks;  // per fast view: (pass, task index)
   cudaGraph_t graph = nullptr;
@@ -1231,7 +1232,7 @@ static void run_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, float*
       if (std::find(E.slow_views.begin(), E.slow_views.end(), (int)v) == E.slow_views.end())
         enqueue_conv(c, E.g[v], imgs[v], outs[v], kers[v], false, ws + E.off[v], plain_layout(E.g[v], false).total,
                      st);
-  } else if (E.schedule == 2) {
+  } else if (E.schedule == 2 || E.schedule == 4) {
     const int P = kBatchStreams;
     while ((int)c.bstreams.size() < P) {
       cudaStream_t s2;
@@ -1245,9 +1246,18 @@ static void run_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, float*
     }
     cuda_check(cudaEventRecord(c.bevents[P], st), "cudaEventRecord");
     for (int i = 0; i < P; ++i) cuda_check(cudaStreamWaitEvent(c.bstreams[i], c.bevents[P], 0), "cudaStreamWaitEvent");
-    for (size_t v = 0; v < E.view_tasks.size(); ++v)
-      for (const auto& pt : E.view_tasks[v])
-        launch_task(E.tasks[pt.first][pt.second], pt.first, c.bstreams[v % P], false);
+    if (E.schedule == 2) {
+      for (size_t v = 0; v < E.view_tasks.size(); ++v)
+        for (const auto& pt : E.view_tasks[v])
+          launch_task(E.tasks[pt.first][pt.second], pt.first, c.bstreams[v % P], false);
+    } else {
+      NoPipeScope np;  // the views' x passes run beside each other
+      int k = 0;
+      for (size_t v = 0; v < E.g.size(); ++v)
+        if (std::find(E.slow_views.begin(), E.slow_views.end(), (int)v) == E.slow_views.end())
+          enqueue_conv(c, E.g[v], imgs[v], outs[v], kers[v], false, ws + E.off[v],
+                       plain_layout(E.g[v], false).total, c.bstreams[k++ % P]);
+    }
     for (int i = 0; i < P; ++i) {
       cuda_check(cudaEventRecord(c.bevents[i], c.bstreams[i]), "cudaEventRecord");
       cuda_check(cudaStreamWaitEvent(st, c.bevents[i], 0), "cudaStreamWaitEvent");
@@ -1289,7 +1299,7 @@ static bool tune_lookup(const std::string& sig, int* choice, int* schedule) {
     for (int i = 0; i < 6; ++i) ok = ok && (bool)(is >> ch[i]);
     if (!ok) continue;
     for (int i = 0; i < 5; ++i) choice[i] = ch[i];
-    if (ch[5] < 0 || ch[5] > 3) continue;
+    if (ch[5] < 0 || ch[5] > 4) continue;
     *schedule = ch[5];
     return true;
   }
@@ -1355,9 +1365,10 @@ static void autotune_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, f
     E.choice[p] = best_choice;
   }
   // whole batch: the tuned pass-major schedule against the view-major and view-concurrent ones
-  static const char* const kSchedName[4] = {"pass-major", "view-major", "view-concurrent", "plain-per-view"};
-  float t_sched[4] = {1e30f, 1e30f, 1e30f, 1e30f};
-  for (int sc = 0; sc < 4; ++sc) {
+  static const char* const kSchedName[5] = {"pass-major", "view-major", "view-concurrent", "plain-per-view",
+                                             "plain-concurrent"};
+  float t_sched[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
+  for (int sc = 0; sc < 5; ++sc) {
     E.schedule = sc;
     for (int r = 0; r < 4; ++r) {
       cuda_check(cudaEventRecord(a, st), "cudaEventRecord");
@@ -1371,7 +1382,7 @@ static void autotune_batch(DevCtx& c, BatchEntry& E, const float* const* imgs, f
     if (tune_log()) std::fprintf(stderr, "fc tune schedule %s: %.1f us\n", kSchedName[sc], 1e3 * t_sched[sc]);
   }
   E.schedule = 0;
-  for (int sc = 1; sc < 4; ++sc)
+  for (int sc = 1; sc < 5; ++sc)
     if (t_sched[sc] < t_sched[E.schedule]) E.schedule = sc;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
@@ -1386,10 +1397,14 @@ static std::string batch_signature(int nv, const int* dims) {
   for (char& ch : name)
     if (ch == ' ') ch = '_';
   std::ostringstream os;
-  os << name << ":v2";
+  os << name << ":v3";  // bumped when the kernels or the schedule set change
   for (int i = 0; i < 6 * nv; ++i) os << (i % 6 == 0 ? ':' : 'x') << dims[i];
   return os.str();
 }
+
+// plan of the most recent batched call on this thread (schedule, per-pass choices)
+static thread_local int t_batch_schedule = -1;
+static thread_local int t_batch_choice[5] = {-1, -1, -1, -1, -1};
 
 static void enqueue_batched(DevCtx& c, int nv, const float* const* imgs, float* const* outs,
                             const float* const* kers, const int* dims, bool compat, char* ws, size_t wsb,
@@ -1470,6 +1485,8 @@ static void enqueue_batched(DevCtx& c, int nv, const float* const* imgs, float* 
   } else {
     E = it->second.get();
   }
+  t_batch_schedule = E->schedule;
+  for (int p = 0; p < 5; ++p) t_batch_choice[p] = E->choice[p];
   if (!use_graphs() || g_prof_on) {
     run_batch(c, *E, imgs, outs, kers, ws, st);
     return;
@@ -2012,6 +2029,12 @@ int fc_conv3d_batched_device(int n_views, const float* const* d_images, float* c
     char* ws = (char*)resolve_ws(c, d_workspace, &wsb, need);
     enqueue_batched(c, n_views, d_images, d_outs, d_kernels, dims, compat, ws, wsb, (cudaStream_t)stream);
   });
+}
+
+int fc_batched_last_plan(int* choices) {
+  if (choices)
+    for (int p = 0; p < 5; ++p) choices[p] = t_batch_choice[p];
+  return t_batch_schedule;
 }
 
 void fc_profile_enable(int on) {

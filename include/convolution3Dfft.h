@@ -204,6 +204,14 @@ FUNCTION_PREFIX int fc_rl_deconvolve_device(const float* d_observed, float* d_es
                                             const float* d_kernel, const int* kernelDim, int iterations, int flags,
                                             void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* Plan the tuner chose for the most recent batched call on this thread:
+ * returns the schedule (0 pass-major, 1 view-major, 2 view-concurrent,
+ * 3 single-volume sequence per view, 4 those sequences concurrently; -1 if
+ * no batched call yet) and, if choices != NULL, the 5 per-pass launch
+ * choices (0 persistent work-list launch, 1 persistent with one CTA per SM,
+ * 2 one launch per view) used by schedules 0-2. */
+FUNCTION_PREFIX int fc_batched_last_plan(int* choices);
+
 /* Per-pass timing: when enabled, every pass records CUDA events on the stream
  * it is launched on.  fc_profile_read synchronises and copies up to max
  * entries (name, milliseconds, algorithmic bytes) of the most recent call(s),

@@ -111,13 +111,13 @@ def test_batched_autotune_cache(cuda, orc, tmp_path):
                 os.environ[k] = v
     text = cache.read_text().strip().splitlines()
     assert len(text) == 1 and len(text[0].split()) == 7
-    assert all(c in "012" for c in text[0].split()[1:6]) and text[0].split()[6] in "0123"
+    assert all(c in "012" for c in text[0].split()[1:6]) and text[0].split()[6] in "01234"
     for (im, k), out in zip(views, outs):
         assert _rel(out.cpu().numpy(), orc.conv_fp64(im, k, "centered")) <= 1e-5
 
 
 def test_batched_every_schedule_and_choice(cuda, orc, tmp_path):
-    """Each schedule (pass-major, view-major, view-concurrent, plain per view) with the
+    """Each schedule (pass-major, view-major, view-concurrent, plain per view, plain concurrent) with the
     persistent work-list launches and with one launch per view, forced through
     the tuning cache; every view against the FP64 oracle."""
     rng = np.random.default_rng(9)
@@ -131,11 +131,15 @@ def test_batched_every_schedule_and_choice(cuda, orc, tmp_path):
         keep.append(_run_batched(cuda, views))
         sig = cache.read_text().split()[0]
         os.environ["FC_AUTOTUNE"] = "0"
-        for sched in (0, 1, 2, 3):
+        for sched in (0, 1, 2, 3, 4):
             for choice in (0, 2):
                 cache.write_text(" ".join([sig] + [str(choice)] * 5 + [str(sched)]) + "\n")
                 imgs, kers, outs = _run_batched(cuda, views)
                 keep.append((imgs, kers, outs))
+                import ctypes
+                from fourierconvolutioncudalib_gb300 import device as fcd
+                ch = (ctypes.c_int * 5)()
+                assert fcd.lib().fc_batched_last_plan(ch) == sched and list(ch) == [choice] * 5
                 for (im, k), out in zip(views, outs):
                     assert _rel(out.cpu().numpy(), orc.conv_fp64(im, k, "centered")) <= 1e-5, (sched, choice)
     finally:
