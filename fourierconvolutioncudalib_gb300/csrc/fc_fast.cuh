@@ -158,7 +158,9 @@ __host__ __device__ constexpr bool lin_read(int NB) {
   return L::D == 0 || NB % L::D == 0;
 }
 
-template <int N, int I, int R, int NS, bool INV, int TCM>
+// stage I of the forward chain (REV = false) or of the reversed chain (REV = true);
+// INV selects the conjugate twiddles and DFT roots
+template <int N, int I, int R, int NS, bool INV, int TCM, bool REV = INV>
 __device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const float2* __restrict__ W,
                                       const TcCtx& tcx) {
   constexpr int U = kVals / R;
@@ -170,7 +172,7 @@ __device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const flo
   for (int b = 0; b < U; ++b) {
     if (NS > 1) {
       const int k = (t + b * A) % NS;
-      const float2* tw = W + Plan<N>::tab_off(INV, I) + k;
+      const float2* tw = W + Plan<N>::tab_off(REV, I) + k;
 #pragma unroll
       for (int r = 1; r < R; ++r) v[b * R + r] = c_tw<INV>(v[b * R + r], __ldg(tw + (r - 1) * NS));
     }
@@ -222,27 +224,30 @@ __device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const 
 }
 
 // stages I .. S-1 of the forward chain (INV = false) or of the reversed chain (INV = true)
-template <int N, int I, int NS, bool INV, int TCM>
+template <int N, int I, int NS, bool INV, int TCM, bool REV = INV>
 struct Chain {
   template <class L>
   static __device__ __forceinline__ void run(float2 (&v)[kVals], const L& sm, const int t,
                                              const float2* __restrict__ W, const TcCtx& tcx) {
-    constexpr int R = Plan<N>::radix(I, INV);
-    stage<N, I, R, NS, INV, TCM>(v, t, W, tcx);
+    constexpr int R = Plan<N>::radix(I, REV);
+    stage<N, I, R, NS, INV, TCM, REV>(v, t, W, tcx);
     if constexpr (I + 1 < Plan<N>::S) {
-      constexpr int R2 = Plan<N>::radix(I + 1, INV);
+      constexpr int R2 = Plan<N>::radix(I + 1, REV);
       exchange<N, R, NS, R2>(v, sm, t);
-      Chain<N, I + 1, NS * R, INV, TCM>::run(v, sm, t, W, tcx);
+      Chain<N, I + 1, NS * R, INV, TCM, REV>::run(v, sm, t, W, tcx);
     }
   }
 };
 
 // full transform; inputs per first_pos, outputs per last_pos.  TCM selects
 // the tensor-core 16-point DFT for the radix-16 stages (tc::kFp16 / kBf16).
-template <int N, bool INV, int TCM = tc::kNone, class L>
+// REV: radix order (false: the forward chain, true: the reversed chain).  An
+// inverse that must consume a forward transform's outputs in registers runs
+// the reversed chain (the default); a standalone inverse pass may run either.
+template <int N, bool INV, int TCM = tc::kNone, bool REV = INV, class L>
 __device__ __forceinline__ void fft(float2 (&v)[kVals], const L& sm, const int t, const float2* __restrict__ W,
                                     const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
-  Chain<N, 0, 1, INV, TCM>::run(v, sm, t, W, tcx);
+  Chain<N, 0, 1, INV, TCM, REV>::run(v, sm, t, W, tcx);
 }
 
 // radix of the first / last stage of the forward (INV=false) or inverse chain

@@ -41,12 +41,14 @@ template <int N>
 using ColGeomWide = ColGeomB<N, 32, 512, 8192>;
 
 // y pass body: tile (bx, plane) = columns [bx*B, bx*B + B) of one plane.
-template <int N, bool INV, class Src, int TCM = tc::kNone, class G = ColGeom<N>>
+// REV: radix order of the transform (a standalone pass may run the inverse in
+// the forward order, which exchanges with fewer shared-memory bank conflicts)
+template <int N, bool INV, class Src, int TCM = tc::kNone, class G = ColGeom<N>, bool REV = INV>
 __device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long ps, long long es, int ncols,
                                           const float2* __restrict__ W, int bx, int plane, int tid, float2* sm,
                                           const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
   constexpr int B = G::B;
-  constexpr int R0 = first_radix<N, INV>(), RF = last_radix<N, INV>();
+  constexpr int R0 = first_radix<N, REV>(), RF = last_radix<N, REV>();
   const int c = tid % B;
   const int t = tid / B;  // >= T for threads beyond the tile: they own no butterfly
   const int col = bx * B + c;
@@ -57,7 +59,7 @@ __device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long
     const int j = stage_pos<N, R0>(t, q);
     v[q] = (ok && j >= 0) ? src.load(plane, j, col) : make_float2(0.f, 0.f);
   }
-  fft<N, INV, TCM>(v, ColLay<B>{sm, c}, t, W, tcx);
+  fft<N, INV, TCM, REV>(v, ColLay<B>{sm, c}, t, W, tcx);
   if (ok) {
     float2* d = dst + (long long)plane * ps + col;
 #pragma unroll
@@ -73,15 +75,16 @@ template <int N, bool INV, class Src>
 __global__ void __launch_bounds__(ColGeomWide<N>::THREADS, 1024 / ColGeomWide<N>::THREADS)
     k_cols_wide(Src src, float2* dst, long long ps, long long es, int ncols, const float2* __restrict__ W) {
   extern __shared__ __align__(16) float2 wsm[];
-  body_cols<N, INV, Src, tc::kNone, ColGeomWide<N>>(src, dst, ps, es, ncols, W, (int)blockIdx.x, (int)blockIdx.y,
-                                                    (int)threadIdx.x, wsm);
+  body_cols<N, INV, Src, tc::kNone, ColGeomWide<N>, false>(src, dst, ps, es, ncols, W, (int)blockIdx.x,
+                                                           (int)blockIdx.y, (int)threadIdx.x, wsm);
 }
 
 template <int N, bool INV, class Src>
 __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* dst, long long ps, long long es,
                                                               int ncols, const float2* __restrict__ W) {
   __shared__ float2 sm[ColGeom<N>::SMEM];
-  body_cols<N, INV>(src, dst, ps, es, ncols, W, (int)blockIdx.x, (int)blockIdx.y, (int)threadIdx.x, sm);
+  body_cols<N, INV, Src, tc::kNone, ColGeom<N>, false>(src, dst, ps, es, ncols, W, (int)blockIdx.x, (int)blockIdx.y,
+                                                      (int)threadIdx.x, sm);
 }
 
 // Fused z pass.  Kernel plane p of KXY holds z = (p - hz) mod nz.  The

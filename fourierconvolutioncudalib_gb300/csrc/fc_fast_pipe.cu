@@ -71,7 +71,8 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
     const RowSlot<N> s(tile, tid, nrows);
     float2 v[kVals];
     if constexpr (C2R)
-      load_c2r<N>(v, TileRows<float2>{reinterpret_cast<const float2*>(buf), tile * P::ROWS, (int)in_pitch}, s);
+      load_c2r<N, TileRows<float2>, false>(
+          v, TileRows<float2>{reinterpret_cast<const float2*>(buf), tile * P::ROWS, (int)in_pitch}, s);
     else
       load_r2c<N>(v, TileRows<float>{reinterpret_cast<const float*>(buf), tile * P::ROWS, (int)in_pitch}, s);
     __syncthreads();  // every thread's reads of the buffer are done
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
       issue(tile + gridDim.x);
     }
     if constexpr (C2R)
-      finish_c2r<N>(v, s, reinterpret_cast<float*>(out), out_pitch, W, sm);
+      finish_c2r<N, tc::kNone, false>(v, s, reinterpret_cast<float*>(out), out_pitch, W, sm);
     else
       finish_r2c<N>(v, s, reinterpret_cast<float2*>(out), out_pitch, W, sm);
   }

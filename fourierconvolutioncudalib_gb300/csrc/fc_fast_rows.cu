@@ -17,7 +17,8 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS) k_c2r(const float2* __res
                                                              float* __restrict__ out, long long out_pitch,
                                                              long long nrows, const float2* __restrict__ W) {
   __shared__ float2 sm[RowGeom<N>::SMEM];
-  body_c2r<N>(in, in_pitch, out, out_pitch, nrows, W, (long long)blockIdx.x, (int)threadIdx.x, sm);
+  body_c2r<N, tc::kNone, false>(in, in_pitch, out, out_pitch, nrows, W, (long long)blockIdx.x, (int)threadIdx.x,
+                                sm);
 }
 
 template <int N, class Src>

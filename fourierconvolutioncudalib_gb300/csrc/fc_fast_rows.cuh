@@ -107,9 +107,12 @@ __device__ __forceinline__ void body_r2c(const Src& src, float2* __restrict__ ou
 
 // first-stage values of the C2R: the Hermitian extension of two half-spectrum
 // rows a, b (read through `in` with row pitch in_pitch), packed as A + i B
-template <int N, class In>
+// REV: radix order of the inverse transform (false: the forward chain with
+// conjugate twiddles, which exchanges with fewer bank conflicts; true: the
+// reversed chain)
+template <int N, class In, bool REV = true>
 __device__ __forceinline__ void load_c2r(float2 (&v)[kVals], const In& in, const RowSlot<N>& s) {
-  constexpr int R0 = first_radix<N, true>();
+  constexpr int R0 = first_radix<N, REV>();
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int k = stage_pos<N, R0>(s.t, q);
@@ -132,13 +135,13 @@ __device__ __forceinline__ void load_c2r(float2 (&v)[kVals], const In& in, const
   }
 }
 
-template <int N, int TCM = tc::kNone>
+template <int N, int TCM = tc::kNone, bool REV = true>
 __device__ __forceinline__ void finish_c2r(float2 (&v)[kVals], const RowSlot<N>& s, float* __restrict__ out,
                                            long long out_pitch, const float2* __restrict__ W, float2* sm,
                                            const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
   using G = RowGeom<N>;
-  constexpr int RF = last_radix<N, true>();
-  fft<N, true, TCM>(v, RowLay{sm + s.line * G::LS}, s.t, W, tcx);
+  constexpr int RF = last_radix<N, REV>();
+  fft<N, true, TCM, REV>(v, RowLay{sm + s.line * G::LS}, s.t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int x = stage_pos<N, RF>(s.t, q);
@@ -156,15 +159,15 @@ struct HalfRows {
   __device__ __forceinline__ float2 load(long long row, int k) const { return p[row * pitch + k]; }
 };
 
-template <int N, int TCM = tc::kNone>
+template <int N, int TCM = tc::kNone, bool REV = true>
 __device__ __forceinline__ void body_c2r(const float2* __restrict__ in, long long in_pitch, float* __restrict__ out,
                                          long long out_pitch, long long nrows, const float2* __restrict__ W,
                                          long long tile, int tid, float2* sm,
                                          const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
   const RowSlot<N> s(tile, tid, nrows);
   float2 v[kVals];
-  load_c2r<N>(v, HalfRows{in, in_pitch}, s);
-  finish_c2r<N, TCM>(v, s, out, out_pitch, W, sm, tcx);
+  load_c2r<N, HalfRows, REV>(v, HalfRows{in, in_pitch}, s);
+  finish_c2r<N, TCM, REV>(v, s, out, out_pitch, W, sm, tcx);
 }
 
 }  // namespace fast

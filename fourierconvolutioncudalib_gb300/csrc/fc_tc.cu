@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_c2r_tc(const float2*
                                                                 long long nrows, const float2* __restrict__ W) {
   extern __shared__ float2 dsm[];
   const TcCtx tcx = tc_setup(dsm + RowGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
-  body_c2r<N, TCM>(in, in_pitch, out, out_pitch, nrows, W, (long long)blockIdx.x, (int)threadIdx.x, dsm, tcx);
+  body_c2r<N, TCM, false>(in, in_pitch, out, out_pitch, nrows, W, (long long)blockIdx.x, (int)threadIdx.x, dsm, tcx);
 }
 
 template <int N, bool INV, class Src>
@@ -52,8 +52,8 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS, 3) k_cols_tc(Src src, flo
                                                                  int ncols, const float2* __restrict__ W) {
   extern __shared__ float2 dsm[];
   const TcCtx tcx = tc_setup(dsm + ColGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
-  body_cols<N, INV, Src, TCM>(src, dst, ps, es, ncols, W, (int)blockIdx.x, (int)blockIdx.y, (int)threadIdx.x, dsm,
-                              tcx);
+  body_cols<N, INV, Src, TCM, ColGeom<N>, false>(src, dst, ps, es, ncols, W, (int)blockIdx.x, (int)blockIdx.y,
+                                                 (int)threadIdx.x, dsm, tcx);
 }
 
 template <int N>
