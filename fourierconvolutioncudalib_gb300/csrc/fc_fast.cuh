@@ -241,9 +241,9 @@ struct Chain {
 
 // full transform; inputs per first_pos, outputs per last_pos.  TCM selects
 // the tensor-core 16-point DFT for the radix-16 stages (tc::kFp16 / kBf16).
-// REV: radix order (false: the forward chain, true: the reversed chain).  An
-// inverse that must consume a forward transform's outputs in registers runs
-// the reversed chain (the default); a standalone inverse pass may run either.
+// REV: radix order (false: the forward chain, true: the reversed chain).  A
+// transform that consumes another's outputs in registers runs the other's
+// order reversed; a standalone pass may run either.
 template <int N, bool INV, int TCM = tc::kNone, bool REV = INV, class L>
 __device__ __forceinline__ void fft(float2 (&v)[kVals], const L& sm, const int t, const float2* __restrict__ W,
                                     const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
