@@ -47,9 +47,9 @@ struct RowSlot {
 };
 
 // first-stage values of the R2C: z = a + i b for real rows a, b of the slot
-template <int N, class Src>
+template <int N, class Src, bool REV = false>
 __device__ __forceinline__ void load_r2c(float2 (&v)[kVals], const Src& src, const RowSlot<N>& s) {
-  constexpr int R0 = first_radix<N, false>();
+  constexpr int R0 = first_radix<N, REV>();
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int x = stage_pos<N, R0>(s.t, q);
@@ -59,16 +59,16 @@ __device__ __forceinline__ void load_r2c(float2 (&v)[kVals], const Src& src, con
 }
 
 // transform of the loaded values, separation of the two half spectra, stores
-template <int N, int TCM = tc::kNone>
+template <int N, int TCM = tc::kNone, bool REV = false>
 __device__ __forceinline__ void finish_r2c(float2 (&v)[kVals], const RowSlot<N>& s, float2* __restrict__ out,
                                            long long out_pitch, const float2* __restrict__ W, float2* sm,
                                            const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
   using G = RowGeom<N>;
-  constexpr int RF = last_radix<N, false>();
+  constexpr int RF = last_radix<N, REV>();
   constexpr int NBF = N / RF, UF = kVals / RF, AF = Plan<N>::A(RF);
   float2* lbase = sm + s.line * G::LS;
   const RowLay lay{lbase};
-  fft<N, false, TCM>(v, lay, s.t, W, tcx);
+  fft<N, false, TCM, REV>(v, lay, s.t, W, tcx);
   // natural-order outputs x = j + m*NBF of the last stage into the line
 #pragma unroll
   for (int b = 0; b < UF; ++b) {
