@@ -69,14 +69,10 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_zconv_tc(float2* __rest
                             (int)threadIdx.x, dsm, stash, T, tcx);
 }
 
+// opt the kernel in to more than 48 KiB of dynamic shared memory where it needs it
 template <class K>
-static cudaError_t launch_dyn(K kernel, dim3 grid, int threads, size_t smem, cudaStream_t st) {
-  if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  (void)grid;
-  (void)threads;
+static cudaError_t allow_smem(K kernel, size_t smem) {
+  if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return cudaSuccess;
 }
 
@@ -102,12 +98,12 @@ cudaError_t FC_TC_NAME(tc_x_r2c, FC_TC_SUFFIX)(const float* in, long long in_pit
     const dim3 grid((unsigned)G::tiles(nrows));                                                                 \
     cudaError_t e;                                                                                              \
     if (taps) {                                                                                                 \
-      e = fast::launch_dyn(fast::k_r2c_tc<n_, SrcBox>, grid, G::THREADS, sm, st);                               \
+      e = fast::allow_smem(fast::k_r2c_tc<n_, SrcBox>, sm);                               \
       if (e != cudaSuccess) return e;                                                                           \
       fast::k_r2c_tc<n_, SrcBox><<<grid, G::THREADS, sm, st>>>(SrcBox{taps, kx, hx, n_}, out, out_pitch, nrows, \
                                                                 ax.W);                                          \
     } else {                                                                                                    \
-      e = fast::launch_dyn(fast::k_r2c_tc<n_, SrcDense>, grid, G::THREADS, sm, st);                             \
+      e = fast::allow_smem(fast::k_r2c_tc<n_, SrcDense>, sm);                             \
       if (e != cudaSuccess) return e;                                                                           \
       fast::k_r2c_tc<n_, SrcDense><<<grid, G::THREADS, sm, st>>>(SrcDense{in, in_pitch}, out, out_pitch, nrows, \
                                                                   ax.W);                                        \
@@ -130,7 +126,7 @@ cudaError_t FC_TC_NAME(tc_x_c2r, FC_TC_SUFFIX)(const float2* in, long long in_pi
     using G = fast::RowGeom<n_>;                                                                     \
     const size_t sm = sizeof(float2) * G::SMEM + fast::tc_bytes(G::THREADS);                         \
     const dim3 grid((unsigned)G::tiles(nrows));                                                      \
-    const cudaError_t e = fast::launch_dyn(fast::k_c2r_tc<n_>, grid, G::THREADS, sm, st);            \
+    const cudaError_t e = fast::allow_smem(fast::k_c2r_tc<n_>, sm);            \
     if (e != cudaSuccess) return e;                                                                  \
     fast::k_c2r_tc<n_><<<grid, G::THREADS, sm, st>>>(in, in_pitch, out, out_pitch, nrows, ax.W);     \
     return cudaGetLastError();                                                                       \
@@ -155,17 +151,17 @@ cudaError_t FC_TC_NAME(tc_cols, FC_TC_SUFFIX)(int mode, const float2* src, long 
     const dim3 grid((ncols + G::B - 1) / G::B, nplanes);                                                         \
     cudaError_t e;                                                                                               \
     if (mode == 2) {                                                                                             \
-      e = fast::launch_dyn(fast::k_cols_tc<n_, false, ColKX>, grid, G::THREADS, sm, st);                         \
+      e = fast::allow_smem(fast::k_cols_tc<n_, false, ColKX>, sm);                         \
       if (e != cudaSuccess) return e;                                                                            \
       fast::k_cols_tc<n_, false, ColKX><<<grid, G::THREADS, sm, st>>>(ColKX{src, src_pitch, krows, hy, n_}, dst, \
                                                                        ps, es, ncols, ax.W);                     \
     } else if (mode == 1) {                                                                                      \
-      e = fast::launch_dyn(fast::k_cols_tc<n_, true, ColPlain>, grid, G::THREADS, sm, st);                       \
+      e = fast::allow_smem(fast::k_cols_tc<n_, true, ColPlain>, sm);                       \
       if (e != cudaSuccess) return e;                                                                            \
       fast::k_cols_tc<n_, true, ColPlain><<<grid, G::THREADS, sm, st>>>(ColPlain{src, ps, es}, dst, ps, es,      \
                                                                           ncols, ax.W);                          \
     } else {                                                                                                     \
-      e = fast::launch_dyn(fast::k_cols_tc<n_, false, ColPlain>, grid, G::THREADS, sm, st);                      \
+      e = fast::allow_smem(fast::k_cols_tc<n_, false, ColPlain>, sm);                      \
       if (e != cudaSuccess) return e;                                                                            \
       fast::k_cols_tc<n_, false, ColPlain><<<grid, G::THREADS, sm, st>>>(ColPlain{src, ps, es}, dst, ps, es,     \
                                                                            ncols, ax.W);                         \
@@ -188,7 +184,7 @@ cudaError_t FC_TC_NAME(tc_zconv, FC_TC_SUFFIX)(float2* S, const float2* KXY, lon
     using G = fast::ColGeom<n_>;                                                                                 \
     const size_t sm = sizeof(float2) * (G::SMEM + G::THREADS * fast::kVals) + fast::tc_bytes(G::THREADS);        \
     const dim3 grid((ncols + G::B - 1) / G::B, ny);                                                              \
-    const cudaError_t e = fast::launch_dyn(fast::k_zconv_tc<n_>, grid, G::THREADS, sm, st);                      \
+    const cudaError_t e = fast::allow_smem(fast::k_zconv_tc<n_>, sm);                      \
     if (e != cudaSuccess) return e;                                                                              \
     fast::k_zconv_tc<n_><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W);       \
     return cudaGetLastError();                                                                                   \

@@ -128,3 +128,30 @@ def test_version_and_cuda_version(fclib):
 
     assert b"sm_103a" in fc.lib().fc_version()
     assert fc.cuda_version() >= 13000
+
+
+def test_reuse_rl_and_batched_plan_entries_without_gpu(fclib):
+    """The kernel-spectrum, Richardson-Lucy and batched-plan entries validate
+    their arguments on the host: sizes grow with the shapes, bad shapes and
+    the compat placement are refused with a status, NULL pointers never reach
+    the device, and no batched call has a plan yet."""
+    import fourierconvolutioncudalib_gb300 as fc
+
+    L = fc.lib()
+    small = L.fc_kernel_spectrum_bytes(fc._iarr([64, 64, 32]), fc._iarr([5, 5, 5]), 0)
+    big = L.fc_kernel_spectrum_bytes(fc._iarr([64, 64, 32]), fc._iarr([5, 5, 9]), 0)
+    assert 0 < small < big  # kernel planes are kept pruned to the kernel's depth
+    assert L.fc_conv3d_kspec_workspace_bytes(fc._iarr([64, 64, 32])) > 0
+    assert L.fc_rl_workspace_bytes(fc._iarr([64, 64, 32]), fc._iarr([5, 5, 5]), 0) > \
+        L.fc_conv3d_kspec_workspace_bytes(fc._iarr([64, 64, 32]))
+    assert L.fc_kernel_spectrum_bytes(fc._iarr([64, 64, 32]), fc._iarr([65, 5, 5]), 0) == 0
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    assert L.fc_kernel_spectrum_bytes(fc._iarr([64, 64, 32]), fc._iarr([5, 5, 5]), fc.FC_FLAG_SHIFT_COMPAT) == 0
+    assert L.fc_last_status() == fc.FC_ERR_UNSUPPORTED
+    assert L.fc_kernel_spectrum_device(None, fc._iarr([5, 5, 5]), fc._iarr([64, 64, 32]), 0, None, 0, None) == \
+        fc.FC_ERR_ARG
+    assert L.fc_conv3d_kspec_device(None, None, fc._iarr([64, 64, 32]), None, fc._iarr([5, 5, 5]), 0, None, 0,
+                                    None) == fc.FC_ERR_ARG
+    assert L.fc_rl_deconvolve_device(None, None, fc._iarr([64, 64, 32]), None, fc._iarr([5, 5, 5]), 3, 0, None, 0,
+                                     None) == fc.FC_ERR_ARG
+    assert L.fc_batched_last_plan(None) == -1
