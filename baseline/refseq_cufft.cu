@@ -1,5 +1,5 @@
-// The reference's convolution3DfftCUDAInPlace restated on cuFFT -- BASELINE
-// AND PARITY HARNESS ONLY, never part of the product library.
+// The reference's convolution3DfftCUDAInPlace restated on cuFFT -- a timing
+// baseline and parity harness only, never part of the product library.
 //
 // The reference sources cannot be built on the GPU host (they are not there),
 // so this file re-expresses the same host and device sequence of
