@@ -10,7 +10,8 @@ set -euo pipefail
 REF=${REF:-/root/reference}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
-[ -d "$REF/src" ] || { echo "reference sources not present" >&2; exit 1; }
+# absent reference tree (e.g. on the GPU host): nothing to build, not an error
+[ -d "$REF/src" ] || { echo "reference sources not present: skipped" >&2; exit 0; }
 mkdir -p "$OUT"
 NVCC=${NVCC:-nvcc}
 FLAGS=(-std=c++17 -O2 --use_fast_math -Xcompiler -fPIC -gencode arch=compute_103a,code=sm_103a
