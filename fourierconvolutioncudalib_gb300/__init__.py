@@ -23,6 +23,7 @@ import numpy as np
 __all__ = [
     "FcError", "lib", "load_library", "library_path",
     "convolution3DfftCUDAInPlace", "convolution3DfftCUDA", "convolution3DfftCUDA_test",
+    "convolution3DfftCUDAInPlaceSaveMemory",
     "selectDeviceWithHighestComputeCapability", "getCUDAcomputeCapabilityMajorVersion",
     "getCUDAcomputeCapabilityMinorVersion", "getNumDevicesCUDA", "getNameDeviceCUDA", "getMemDeviceCUDA",
     "cuda_version", "gpu_mem_needed_mb", "plan_radices",
@@ -63,6 +64,7 @@ _SIGNATURES = {
     "convolution3DfftCUDA_test": (_FP, [_FP, _IP, _FP, _I]),
     "convolution3DfftCUDA": (_FP, [_FP, _IP, _FP, _IP, _I]),
     "convolution3DfftCUDAInPlace": (None, [_FP, _IP, _FP, _IP, _I]),
+    "convolution3DfftCUDAInPlaceSaveMemory": (None, [_FP, _IP, _FP, _IP, _I]),
     "selectDeviceWithHighestComputeCapability": (_I, []),
     "getCUDAcomputeCapabilityMinorVersion": (_I, [_I]),
     "getCUDAcomputeCapabilityMajorVersion": (_I, [_I]),
@@ -87,6 +89,8 @@ _SIGNATURES = {
     "fc_conv3d_kspec_workspace_bytes": (_SZ, [_IP]),
     "fc_conv3d_kspec_device": (_I, [_P, _P, _IP, _P, _IP, _I, _P, _SZ, _P]),
     "fc_rl_workspace_bytes": (_SZ, [_IP, _IP, _I]),
+    "fc_conv3d_subsampled_workspace_bytes": (_SZ, [_IP, _IP]),
+    "fc_conv3d_subsampled_device": (_I, [_P, _P, _IP, _P, _IP, _P, _SZ, _P]),
     "fc_rl_deconvolve_device": (_I, [_P, _P, _IP, _P, _IP, _I, _I, _P, _SZ, _P]),
     "fc_conv3d_adjoint_workspace_bytes": (_SZ, [_IP, _IP, _I]),
     "fc_conv3d_adjoint_device": (_I, [_P, _P, _P, _P, _P, _IP, _IP, _I, _P, _SZ, _P]),
@@ -162,6 +166,22 @@ def convolution3DfftCUDAInPlace(im: np.ndarray, imDim: Sequence[int], kernel: np
     if im.size != int(np.prod(imDim)) or kernel.size != int(np.prod(kernelDim)):
         raise FcError(FC_ERR_ARG, "array sizes do not match the given dimensions")
     lib().convolution3DfftCUDAInPlace(_fptr(im), _iarr(imDim), _fptr(kernel), _iarr(kernelDim), int(devCUDA))
+    _check()
+
+
+def convolution3DfftCUDAInPlaceSaveMemory(im: np.ndarray, imDim: Sequence[int], kernel: np.ndarray,
+                                          kernelDim: Sequence[int], devCUDA: int) -> None:
+    """Overwrite ``im`` with the subsampled-kernel approximation of its
+    convolution by ``kernel``: the kernel's spectrum at its own size, read at
+    the nearest kernel frequency of each image frequency (reference
+    src/convolution3Dfft.h:58-64, src/convolution3Dfft.cu:65-125).  Same
+    dimension order and errors as convolution3DfftCUDAInPlace."""
+    _as_f32c(im, "im")
+    _as_f32c(kernel, "kernel")
+    if im.size != int(np.prod(imDim)) or kernel.size != int(np.prod(kernelDim)):
+        raise FcError(FC_ERR_ARG, "array sizes do not match the given dimensions")
+    lib().convolution3DfftCUDAInPlaceSaveMemory(_fptr(im), _iarr(imDim), _fptr(kernel), _iarr(kernelDim),
+                                                int(devCUDA))
     _check()
 
 

@@ -27,7 +27,7 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hi
 SOURCES = [(f, Path(f).stem, []) for f in [
     "fc_host.cpp", "fc_kernels.cu", "fc_fast_rows.cu", "fc_fast_cols.cu", "fc_fast_zconv.cu", "fc_fast_zadj.cu",
     "fc_batched_rows_fwd.cu", "fc_batched_rows_inv.cu", "fc_batched_cols_fwd.cu", "fc_batched_cols_inv.cu",
-    "fc_batched_zconv.cu", "fc_noalloc.cu", "fc_fast_pipe.cu"]] + [
+    "fc_batched_zconv.cu", "fc_noalloc.cu", "fc_fast_pipe.cu", "fc_fast_zsub.cu"]] + [
     ("fc_tc.cu", "fc_tc_fp16", ["-DFC_TC_MODE=1"]), ("fc_tc.cu", "fc_tc_bf16", ["-DFC_TC_MODE=2"])]
 
 

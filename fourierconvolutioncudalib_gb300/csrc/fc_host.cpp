@@ -228,12 +228,23 @@ static Tiles choose_tiles(const Geom& g) {
   // x passes: about 2048 complex values per CTA (two real rows per line)
   long long P = std::max(1LL, 2048LL / std::max(1, g.nx));
   P = std::min(P, 64LL);
+  // small volumes (a kernel transformed at its own size): fewer line pairs
+  // per CTA, so that the grid still gives every SM two CTAs (each line's
+  // transform does not depend on the tiling)
+  const long long kMinCtas = 2 * 152;
+  const long long rows = (long long)g.ny * g.nz;
+  while (P > 1 && (rows + 2 * P - 1) / (2 * P) < kMinCtas) P >>= 1;
   t.x_pairs_log2 = ilog2_floor(P);
-  // y passes: about 4096 complex values per tile (64 KiB of shared memory for 2 buffers)
+  // y passes: about 4096 complex values per tile (64 KiB of shared memory for 2 buffers),
+  // no wider than the spectrum's columns
   long long By = std::max(1LL, std::min(32LL, 4096LL / std::max(1, g.ny)));
+  while (By > 1 && By / 2 >= g.nxh) By >>= 1;
+  while (By > 1 && (g.nxh + By - 1) / By * g.nz < kMinCtas) By >>= 1;
   t.y_cols_log2 = ilog2_floor(By);
   // z pass holds image and kernel columns: about 2048 columns x rows
   long long Bz = std::max(1LL, std::min(32LL, 2048LL / std::max(1, g.nz)));
+  while (Bz > 1 && Bz / 2 >= g.nxh) Bz >>= 1;
+  while (Bz > 1 && (g.nxh + Bz - 1) / Bz * g.ny < kMinCtas) Bz >>= 1;
   t.z_cols_log2 = ilog2_floor(Bz);
   return t;
 }
@@ -871,6 +882,85 @@ static void enqueue_irfft3d(DevCtx& c, const Geom& g, const float* d_spec, float
   enqueue_yx_inv(g, a, t, S, d_out, st, "fft_y_inv", "fft_x_c2r");
 }
 
+// ------------------------------------------------------------------ subsampled kernel
+// The memory-saving variant whose device product the reference keeps
+// (src/convolution3Dfft.cu:65-125) behind a commented-out entry point
+// (src/convolution3Dfft.h:58-64): the kernel is transformed at its own size,
+// unpadded and unshifted, and each image frequency takes the nearest kernel
+// frequency (fc_sub.cuh).  Workspace: S (image spectrum), then K (the
+// kernel's spectrum, kx/2+1 columns of its own pitch, ky rows, kz planes).
+struct SubLayout {
+  size_t off_K, total;
+};
+static Geom sub_kernel_geom(const Geom& g) { return make_geom(g.kx, g.ky, g.kz, 0, 0, 0, true); }
+static SubLayout sub_layout(const Geom& g) {
+  SubLayout L;
+  L.off_K = image_ws_bytes(g);
+  L.total = L.off_K + image_ws_bytes(sub_kernel_geom(g));
+  return L;
+}
+
+static void enqueue_conv_sub(DevCtx& c, const Geom& g, const float* d_image, float* d_out, const float* d_kernel,
+                             char* ws, size_t ws_bytes, cudaStream_t st) {
+  const SubLayout L = sub_layout(g);
+  if (ws_bytes < L.total) FC_THROW(FC_ERR_NOMEM, "workspace too small");
+  const Geom kg = sub_kernel_geom(g);
+  const Tiles t = choose_tiles(g), tk = choose_tiles(kg);
+  const Axes a = axes_for(c, g), ak = axes_for(c, kg);
+  float2* S = (float2*)ws;
+  float2* K = (float2*)(ws + L.off_K);
+  // the kernel's passes (a few latency-bound launches) run on the side stream
+  // beside the image y pass, forked after the image x pass as in the plain
+  // convolution, and without the persistent x kernel
+  auto kernel_passes = [&](cudaStream_t ks) {
+    NoPipeScope np;
+    enqueue_xy_fwd(kg, ak, tk, d_kernel, K, ks, "sub_kernel_x_r2c", "sub_kernel_y_fwd");
+    FC_PASS("sub_kernel_z_fwd", 16.0 * kg.nxh * (double)kg.ny * kg.nz, ks,
+            d_cols(K, K, kg.pitch, (long long)kg.ny * kg.pitch, kg.nxh, kg.ny, false, ak.z, tk.z_cols_log2,
+                   tk.threads, ks));
+  };
+  const long long rows = (long long)g.ny * g.nz;
+  FC_PASS("image_x_r2c", 4.0 * g.N() + 8.0 * g.nxh * rows, st,
+          d_x_r2c_dense(d_image, g.nx, S, g.pitch, rows, a.x, t, st));
+  const bool fork = use_fork();
+  Fork f{};
+  if (fork) {
+    f = ctx_fork(c);
+    cuda_check(cudaEventRecord(f.forked, st), "cudaEventRecord(fork)");
+    cuda_check(cudaStreamWaitEvent(f.side, f.forked, 0), "cudaStreamWaitEvent(fork)");
+    kernel_passes(f.side);
+    cuda_check(cudaEventRecord(f.joined, f.side), "cudaEventRecord(join)");
+  } else {
+    kernel_passes(st);
+  }
+  FC_PASS("image_y_fwd", 16.0 * g.nxh * (double)rows, st,
+          d_cols(S, S, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, false, a.y, t.y_cols_log2, t.threads, st));
+  if (fork) cuda_check(cudaStreamWaitEvent(st, f.joined, 0), "cudaStreamWaitEvent(join)");
+  SubMap m;
+  m.K = K;
+  m.kpitch = kg.pitch;
+  m.kx = g.kx;
+  m.ky = g.ky;
+  m.kz = g.kz;
+  m.kxh = kg.nxh;
+  // r = kernel extent / image extent (src/convolution3Dfft.cu:68-70), IEEE division
+  m.rx = (float)g.kx / (float)g.nx;
+  m.ry = (float)g.ky / (float)g.ny;
+  m.rz = (float)g.kz / (float)g.nz;
+  const float scale = 1.0f / (float)g.N();
+  const double zbytes = 16.0 * g.nxh * (double)g.ny * g.nz;
+  if (use_fast() && fast_cols_supported(g.nz)) {
+    FC_PASS("zsub", zbytes, st, fast_zsub(S, g.pitch, g.ny, g.nxh, m, scale, a.z, st));
+  } else {
+    const long long es = (long long)g.ny * g.pitch;
+    FC_PASS("sub_z_fwd", zbytes, st,
+            d_cols(S, S, g.pitch, es, g.nxh, g.ny, false, a.z, t.z_cols_log2, t.threads, st));
+    FC_PASS("sub_modulate", zbytes, st, launch_sub_modulate(S, g.pitch, g.ny, g.nz, g.nxh, m, scale, st));
+    FC_PASS("sub_z_inv", zbytes, st, d_cols(S, S, g.pitch, es, g.nxh, g.ny, true, a.z, t.z_cols_log2, t.threads, st));
+  }
+  enqueue_yx_inv(g, a, t, S, d_out, st, "image_y_inv", "image_x_c2r");
+}
+
 // ------------------------------------------------------------------ host entry points
 static void set_device(int dev) {
   int n = 0;
@@ -922,15 +1012,21 @@ static bool host_buffer_pinned(const void* p) {
 
 // Host-pointer convolution used by the three reference-compatible entry points.
 static void host_conv(const float* im, float* out, int nx, int ny, int nz, const float* kernel, int kx, int ky,
-                      int kz, bool dense, int dev, bool allow_direct = false) {
+                      int kz, bool dense, int dev, bool allow_direct = false, bool subsampled = false) {
   if (!im || !out || !kernel) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
   const Geom g = make_geom(nx, ny, nz, kx, ky, kz, dense);
   set_device(dev);
-  const bool compat = shift_compat_default() && g.kbox;
+  const bool compat = !subsampled && shift_compat_default() && g.kbox;
   DevCtx& c = ctx_for(dev);
   std::lock_guard<std::mutex> lk(c.mu);
   cudaStream_t st = ctx_stream(c);
-  const size_t wsb = plain_layout(g, compat).total;
+  const size_t wsb = subsampled ? sub_layout(g).total : plain_layout(g, compat).total;
+  auto run = [&](const float* src, float* dst) {
+    if (subsampled)
+      enqueue_conv_sub(c, g, src, dst, c.d_ker, (char*)c.ws, c.ws_cap, st);
+    else
+      enqueue_conv(c, g, src, dst, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
+  };
   const size_t nimg = sizeof(float) * (size_t)g.N();
   const size_t nker = sizeof(float) * (dense ? (size_t)g.N() : (size_t)kx * ky * kz);
   grow(&c.ws, &c.ws_cap, wsb, "cudaMalloc(workspace)");
@@ -940,7 +1036,7 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
   if (allow_direct && mode != 0 && device_reads_pageable(dev) && (mode == 1 || host_buffer_pinned(im))) {
     {
       HostSrcScope hs(true);
-      enqueue_conv(c, g, im, out, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
+      run(im, out);
     }
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     if (pipe_take_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in a pipelined pass");
@@ -948,7 +1044,7 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
   }
   grow((void**)&c.d_img, &c.img_cap, nimg, "cudaMalloc(image)");
   cuda_check(cudaMemcpyAsync(c.d_img, im, nimg, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(image H2D)");
-  enqueue_conv(c, g, c.d_img, c.d_img, c.d_ker, compat, (char*)c.ws, c.ws_cap, st);
+  run(c.d_img, c.d_img);
   cuda_check(cudaMemcpyAsync(out, c.d_img, nimg, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync(result D2H)");
   cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   if (pipe_take_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in a pipelined pass");
@@ -1636,6 +1732,16 @@ void convolution3DfftCUDAInPlace(imageType* im, int* imDim, imageType* kernel, i
   });
 }
 
+void convolution3DfftCUDAInPlaceSaveMemory(imageType* im, int* imDim, imageType* kernel, int* kernelDim, int devCUDA) {
+  clear_status();
+  guarded([&] {
+    int nx, ny, nz, kx, ky, kz;
+    dims3(imDim, &nx, &ny, &nz);
+    dims3(kernelDim, &kx, &ky, &kz);
+    host_conv(im, im, nx, ny, nz, kernel, kx, ky, kz, false, devCUDA, true, true);
+  });
+}
+
 int getNumDevicesCUDA(void) {
   clear_status();
   int n = 0;
@@ -1801,6 +1907,35 @@ int fc_conv3d_device(const float* d_image, float* d_out, const int* imDim, const
     size_t wsb = workspace_bytes;
     void* ws = resolve_ws(c, d_workspace, &wsb, plain_layout(g, compat).total);
     enqueue_conv(c, g, d_image, d_out, d_kernel, compat, (char*)ws, wsb, (cudaStream_t)stream);
+  });
+}
+
+size_t fc_conv3d_subsampled_workspace_bytes(const int* imDim, const int* kernelDim) {
+  clear_status();
+  size_t r = 0;
+  guarded([&] {
+    int nx, ny, nz, kx, ky, kz;
+    dims3(imDim, &nx, &ny, &nz);
+    dims3(kernelDim, &kx, &ky, &kz);
+    r = sub_layout(make_geom(nx, ny, nz, kx, ky, kz, false)).total;
+  });
+  return r;
+}
+
+int fc_conv3d_subsampled_device(const float* d_image, float* d_out, const int* imDim, const float* d_kernel,
+                                const int* kernelDim, void* d_workspace, size_t workspace_bytes, void* stream) {
+  clear_status();
+  return guarded([&] {
+    if (!d_image || !d_out || !d_kernel) FC_THROW(FC_ERR_ARG, "NULL pointer argument");
+    int nx, ny, nz, kx, ky, kz;
+    dims3(imDim, &nx, &ny, &nz);
+    dims3(kernelDim, &kx, &ky, &kz);
+    const Geom g = make_geom(nx, ny, nz, kx, ky, kz, false);
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    size_t wsb = workspace_bytes;
+    void* ws = resolve_ws(c, d_workspace, &wsb, sub_layout(g).total);
+    enqueue_conv_sub(c, g, d_image, d_out, d_kernel, (char*)ws, wsb, (cudaStream_t)stream);
   });
 }
 

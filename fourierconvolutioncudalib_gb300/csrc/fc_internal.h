@@ -78,6 +78,20 @@ cudaError_t launch_rl_update(float* x, const float* v, long long n, cudaStream_t
 cudaError_t launch_crop_kernel(const float* vol, long long row_pitch, int ny_rows, int nx, int kx, int ky, int kz,
                                float* out, cudaStream_t st);
 
+// Subsampled-kernel product (src/convolution3Dfft.cu:65-125): the kernel's
+// spectrum at its own size (kx/2+1 columns of pitch kpitch, ky rows, kz
+// planes; unshifted taps), read at the nearest kernel frequency of each image
+// frequency (fc_sub.cuh).  r = k / n per axis, in float32.
+struct SubMap {
+  const float2* K;
+  long long kpitch;
+  int kx, ky, kz, kxh;
+  float rx, ry, rz;
+};
+// S[z][y][x] = scale * (coeff * S) over nz planes of ny rows of ncols columns (pitch)
+cudaError_t launch_sub_modulate(float2* S, long long pitch, int ny, int nz, int ncols, const SubMap& m, float scale,
+                                cudaStream_t st);
+
 // Register-resident fast path for power-of-two lengths (fc_fast_rows.cu,
 // fc_fast_cols.cu).  Same contracts as the generic launchers above; they
 // return cudaErrorNotSupported for lengths they do not cover.
@@ -121,6 +135,9 @@ cudaError_t fast_zconv(float2* S, const float2* KXY, long long pitch, int ny, in
                        float scale, bool conj_kernel, const FcAxis& az, cudaStream_t st);
 cudaError_t fast_zcorr(const float2* X, const float2* G, float2* out, long long pitch, int ny, int ncols, int kz,
                        int hz, float scale, const FcAxis& az, cudaStream_t st);
+// fused subsampled-kernel z pass: z forward, launch_sub_modulate's product, z inverse
+cudaError_t fast_zsub(float2* S, long long pitch, int ny, int ncols, const SubMap& m, float scale, const FcAxis& az,
+                      cudaStream_t st);
 
 // Tensor-core precision mode (fc_tc.cu, compiled for fp16 and for bf16):
 // register-resident kernels whose radix-16 stages run on the tensor cores,

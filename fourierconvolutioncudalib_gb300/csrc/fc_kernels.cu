@@ -17,6 +17,7 @@
 #include "fc_internal.h"
 #include "fc_fft.cuh"
 #include "fc_sources.cuh"
+#include "fc_sub.cuh"
 
 namespace fc {
 
@@ -34,30 +35,27 @@ __global__ void __launch_bounds__(256) k_x_r2c(Src src, float2* __restrict__ out
   float2* B = smem + P * ls;
   const long long row0 = (long long)blockIdx.x * 2 * P;
 
-  for (int p = 0; p < P; ++p) {
+  // (line, x) flattened over the CTA: short rows keep every thread busy
+  for (int e = threadIdx.x; e < P * n; e += blockDim.x) {
+    const int p = e / n, x = e - p * n;
     const long long ra = row0 + 2 * p, rb = ra + 1;
-    const bool va = ra < nrows, vb = rb < nrows;
-#pragma unroll 4
-    for (int x = threadIdx.x; x < n; x += blockDim.x) {
-      const float a = va ? src.load(ra, x) : 0.f;
-      const float b = vb ? src.load(rb, x) : 0.f;
-      A[p * ls + x] = make_float2(a, b);
-    }
+    const float a = ra < nrows ? src.load(ra, x) : 0.f;
+    const float b = rb < nrows ? src.load(rb, x) : 0.f;
+    A[p * ls + x] = make_float2(a, b);
   }
   __syncthreads();
   const float2* R = fc_fft_lines<false>(A, B, ax, pairs_log2, 1, ls);
   const int nh = n / 2 + 1;
-  for (int p = 0; p < P; ++p) {
+  for (int e = threadIdx.x; e < P * nh; e += blockDim.x) {
+    const int p = e / nh, k = e - p * nh;
     const long long ra = row0 + 2 * p, rb = ra + 1;
     const bool va = ra < nrows, vb = rb < nrows;
-    for (int k = threadIdx.x; k < nh; k += blockDim.x) {
-      const float2 zk = R[p * ls + k];
-      const float2 zn = R[p * ls + (k == 0 ? 0 : n - k)];
-      const float2 Ak = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
-      const float2 Bk = make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x));
-      if (va) out[ra * out_pitch + k] = Ak;
-      if (vb) out[rb * out_pitch + k] = Bk;
-    }
+    const float2 zk = R[p * ls + k];
+    const float2 zn = R[p * ls + (k == 0 ? 0 : n - k)];
+    const float2 Ak = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+    const float2 Bk = make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x));
+    if (va) out[ra * out_pitch + k] = Ak;
+    if (vb) out[rb * out_pitch + k] = Bk;
   }
 }
 
@@ -78,36 +76,33 @@ __global__ void __launch_bounds__(256) k_x_c2r(const float2* __restrict__ in, lo
   const int nh = n / 2 + 1;
   const bool even = (n & 1) == 0;
 
-  for (int p = 0; p < P; ++p) {
+  for (int e = threadIdx.x; e < P * n; e += blockDim.x) {
+    const int p = e / n, k = e - p * n;
     const long long ra = row0 + 2 * p, rb = ra + 1;
     const bool va = ra < nrows, vb = rb < nrows;
-#pragma unroll 4
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      const bool lo = k < nh;
-      const int kk = lo ? k : n - k;
-      float2 a = va ? in[ra * in_pitch + kk] : make_float2(0.f, 0.f);
-      float2 b = vb ? in[rb * in_pitch + kk] : make_float2(0.f, 0.f);
-      if (kk == 0 || (even && kk == n / 2)) {
-        a.y = 0.f;
-        b.y = 0.f;
-      }
-      if (!lo) {
-        a.y = -a.y;
-        b.y = -b.y;
-      }
-      A[p * ls + k] = make_float2(a.x - b.y, a.y + b.x);
+    const bool lo = k < nh;
+    const int kk = lo ? k : n - k;
+    float2 a = va ? in[ra * in_pitch + kk] : make_float2(0.f, 0.f);
+    float2 b = vb ? in[rb * in_pitch + kk] : make_float2(0.f, 0.f);
+    if (kk == 0 || (even && kk == n / 2)) {
+      a.y = 0.f;
+      b.y = 0.f;
     }
+    if (!lo) {
+      a.y = -a.y;
+      b.y = -b.y;
+    }
+    A[p * ls + k] = make_float2(a.x - b.y, a.y + b.x);
   }
   __syncthreads();
   const float2* R = fc_fft_lines<true>(A, B, ax, pairs_log2, 1, ls);
-  for (int p = 0; p < P; ++p) {
+  for (int e = threadIdx.x; e < P * n; e += blockDim.x) {
+    const int p = e / n, x = e - p * n;
     const long long ra = row0 + 2 * p, rb = ra + 1;
     const bool va = ra < nrows, vb = rb < nrows;
-    for (int x = threadIdx.x; x < n; x += blockDim.x) {
-      const float2 z = R[p * ls + x];
-      if (va) out[ra * out_pitch + x] = z.x;
-      if (vb) out[rb * out_pitch + x] = z.y;
-    }
+    const float2 z = R[p * ls + x];
+    if (va) out[ra * out_pitch + x] = z.x;
+    if (vb) out[rb * out_pitch + x] = z.y;
   }
 }
 
@@ -501,6 +496,29 @@ cudaError_t launch_rl_update(float* x, const float* v, long long n, cudaStream_t
   if (n <= 0) return cudaSuccess;
   const bool vec = (((uintptr_t)x | (uintptr_t)v) & 15) == 0;
   k_rl_update<<<pointwise_grid(n), 256, 0, st>>>(x, v, n, vec);
+  return cudaGetLastError();
+}
+
+// subsampled-kernel product over the spectrum (element (z, y, x) of the
+// padded layout; the reference's flat index decomposition at :80-84)
+__global__ void k_sub_modulate(float2* __restrict__ S, long long pitch, int ny, int nz, int ncols, SubMap m,
+                               float scale) {
+  const long long n = (long long)nz * ny * ncols;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int x = (int)(i % ncols);
+    const long long r = i / ncols;  // row z * ny + y
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    float2* p = S + r * pitch + x;
+    *p = sub_product(SubCol(m, x, y).at(z), *p, scale);
+  }
+}
+
+cudaError_t launch_sub_modulate(float2* S, long long pitch, int ny, int nz, int ncols, const SubMap& m, float scale,
+                                cudaStream_t st) {
+  const long long n = (long long)nz * ny * ncols;
+  if (n <= 0) return cudaSuccess;
+  k_sub_modulate<<<pointwise_grid(n), 256, 0, st>>>(S, pitch, ny, nz, ncols, m, scale);
   return cudaGetLastError();
 }
 

@@ -15,7 +15,8 @@ import torch
 from . import FC_FLAG_CORRELATE, FC_FLAG_DENSE_KERNEL, FcError, FC_ERR_ARG, _check, _iarr, lib
 
 __all__ = ["conv3d", "conv3d_adjoint", "conv3d_batched", "rfft3d", "irfft3d", "pad_shift_kernel",
-           "kernel_spectrum", "conv3d_kspec", "rl_deconvolve", "workspace_bytes", "profile", "launch_count"]
+           "kernel_spectrum", "conv3d_kspec", "rl_deconvolve", "conv3d_subsampled", "subsampled_workspace_bytes",
+           "workspace_bytes", "profile", "launch_count"]
 
 
 def _dims(t: torch.Tensor) -> Tuple[int, int, int]:
@@ -141,6 +142,37 @@ def rl_deconvolve(observed: torch.Tensor, kernel: torch.Tensor, iterations: int,
     _check(lib().fc_rl_deconvolve_device(observed.data_ptr(), estimate.data_ptr(), _iarr([nx, ny, nz]),
                                          kernel.data_ptr(), kd, int(iterations), int(flags), wp, wb, _stream(stream)))
     return estimate
+
+
+def subsampled_workspace_bytes(image_shape: Sequence[int], kernel_shape: Sequence[int]) -> int:
+    """Bytes of scratch for conv3d_subsampled; shapes are torch order (z, y, x)."""
+    nz, ny, nx = image_shape
+    kz, ky, kx = kernel_shape
+    n = lib().fc_conv3d_subsampled_workspace_bytes(_iarr([nx, ny, nz]), _iarr([kx, ky, kz]))
+    if n == 0:
+        _check()
+    return int(n)
+
+
+def conv3d_subsampled(image: torch.Tensor, kernel: torch.Tensor, out: Optional[torch.Tensor] = None,
+                      workspace: Optional[torch.Tensor] = None,
+                      stream: Optional[torch.cuda.Stream] = None) -> torch.Tensor:
+    """Subsampled-kernel approximation of the convolution of image [nz,ny,nx]
+    by kernel [kz,ky,kx] (fc_conv3d_subsampled_device): the kernel's spectrum
+    at its own size, read at the nearest kernel frequency of each image
+    frequency."""
+    _f32(image, "image")
+    _f32(kernel, "kernel")
+    nx, ny, nz = _dims(image)
+    kx, ky, kz = _dims(kernel)
+    if out is None:
+        out = torch.empty_like(image)
+    _f32(out, "out")
+    need = subsampled_workspace_bytes((nz, ny, nx), (kz, ky, kx))
+    wp, wb = _ws(workspace, need, image.device)
+    _check(lib().fc_conv3d_subsampled_device(image.data_ptr(), out.data_ptr(), _iarr([nx, ny, nz]),
+                                             kernel.data_ptr(), _iarr([kx, ky, kz]), wp, wb, _stream(stream)))
+    return out
 
 
 def conv3d_adjoint(image: Optional[torch.Tensor], kernel: Optional[torch.Tensor], grad_out: torch.Tensor,

@@ -56,6 +56,20 @@ FUNCTION_PREFIX imageType* convolution3DfftCUDA(imageType* im, int* imDim, image
 FUNCTION_PREFIX void convolution3DfftCUDAInPlace(imageType* im, int* imDim, imageType* kernel, int* kernelDim,
                                                  int devCUDA);
 
+/* Replaces reference src/convolution3Dfft.h:58-64, the commented-out
+ * convolution3DfftCUDAInPlaceSaveMemory, whose device product survives as
+ * modulateAndNormalizeSubsampled_kernel (src/convolution3Dfft.cu:65-125).
+ * Same arguments and error behaviour as convolution3DfftCUDAInPlace; the
+ * kernel is transformed at its own size (no padding, no centring) and each
+ * image frequency takes the nearest kernel frequency, (int)(r*f + 0.5) mod k
+ * per axis with r = k/n, negated where the three kernel indices sum to an odd
+ * number.  An approximation of the convolution (the reference states 2 %
+ * maximum relative error for images larger than 5x the kernel); for an odd kx
+ * the x index (kx+1)/2 takes the Hermitian mirror of the stored half spectrum
+ * (the reference reads past its row there). */
+FUNCTION_PREFIX void convolution3DfftCUDAInPlaceSaveMemory(imageType* im, int* imDim, imageType* kernel,
+                                                           int* kernelDim, int devCUDA);
+
 /* Replace reference src/convolution3Dfft.h:66-72 (bodies src/standardCUDAfunctions.cu:13-71,
  * src/convolution3Dfft.cu:581-584).  On failure the int queries return -1
  * (selectDevice..., compute capability) or 0 (device count, memory). */
@@ -203,6 +217,17 @@ FUNCTION_PREFIX size_t fc_rl_workspace_bytes(const int* imDim, const int* kernel
 FUNCTION_PREFIX int fc_rl_deconvolve_device(const float* d_observed, float* d_estimate, const int* imDim,
                                             const float* d_kernel, const int* kernelDim, int iterations, int flags,
                                             void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Device-pointer form of convolution3DfftCUDAInPlaceSaveMemory: d_out may
+ * equal d_image; imDim = {nx, ny, nz}, kernelDim = {kx, ky, kz} with the
+ * kernel no larger than the image along any axis.  Workspace:
+ * fc_conv3d_subsampled_workspace_bytes (the image spectrum plus the kernel's
+ * own-size spectrum), 256-byte aligned, or NULL for the library's own.
+ * Asynchronous on `stream`. */
+FUNCTION_PREFIX size_t fc_conv3d_subsampled_workspace_bytes(const int* imDim, const int* kernelDim);
+FUNCTION_PREFIX int fc_conv3d_subsampled_device(const float* d_image, float* d_out, const int* imDim,
+                                                const float* d_kernel, const int* kernelDim, void* d_workspace,
+                                                size_t workspace_bytes, void* stream);
 
 /* Plan the tuner chose for the most recent batched call on this thread:
  * returns the schedule (0 pass-major, 1 view-major, 2 view-concurrent,

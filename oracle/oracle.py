@@ -219,6 +219,48 @@ def correlate_fp64(image: np.ndarray, kernel: np.ndarray) -> np.ndarray:
     return np.fft.irfftn(a * np.conj(np.fft.rfftn(pk)), s=image.shape, axes=(0, 1, 2))
 
 
+def subsampled_index(n: int, k: int, m: int) -> np.ndarray:
+    """Kernel frequency read by image frequencies 0..m-1 of an axis of length n
+    (src/convolution3Dfft.cu:68-70, :106-108): (int)(r*f + 0.5f) % k with
+    r = (float)k / (float)n in float32 and the multiply-add rounded once (the
+    contracted expression).  r*f + 0.5 is exact in float64 (24-bit r times an
+    integer below 2**13), so one cast to float32 is the fused rounding."""
+    r = np.float32(np.float32(k) / np.float32(n))
+    f = np.arange(m, dtype=np.float64)
+    v = (np.float64(r) * f + 0.5).astype(np.float32)
+    return np.trunc(v).astype(np.int64) % k
+
+
+def subsampled_coefficients(kernel: np.ndarray, image_shape_zyx: Sequence[int]) -> np.ndarray:
+    """The kernel coefficient of every image frequency of the subsampled-kernel
+    product (src/convolution3Dfft.cu:65-125) in double precision: the
+    spectrum of the unpadded, unshifted kernel at its own size, read at the
+    nearest-neighbour indices, negated where the three indices sum to an odd
+    number (:113-117).  The full spectrum is indexed, so an x index past the
+    stored half (odd kx, at the image's x Nyquist) takes the Hermitian mirror;
+    the reference reads past its half-spectrum row there."""
+    nz, ny, nx = image_shape_zyx
+    kz, ky, kx = kernel.shape
+    K = np.fft.fftn(np.asarray(kernel, np.float64))
+    iz = subsampled_index(nz, kz, nz)
+    iy = subsampled_index(ny, ky, ny)
+    ix = subsampled_index(nx, kx, nx // 2 + 1)
+    A = K[np.ix_(iz, iy, ix)]
+    odd = (iz[:, None, None] + iy[None, :, None] + ix[None, None, :]) % 2 == 1
+    return np.where(odd, -A, A)
+
+
+def subsampled_fp64(image: np.ndarray, kernel: np.ndarray) -> np.ndarray:
+    """FP64 oracle of the subsampled-kernel convolution: the image's half
+    spectrum times subsampled_coefficients, inverse real transform.  Where the
+    product is not Hermitian on the x DC and Nyquist planes, the imaginary
+    parts of those bins are dropped after the z and y inverses (numpy's irfftn,
+    and the library's C2R passes)."""
+    x = np.asarray(image, np.float64)
+    A = subsampled_coefficients(kernel, x.shape)
+    return np.fft.irfftn(np.fft.rfftn(x) * A, s=x.shape, axes=(0, 1, 2))
+
+
 def rl_fp64(observed: np.ndarray, kernel: np.ndarray, iterations: int,
             estimate: Optional[np.ndarray] = None) -> np.ndarray:
     """Richardson-Lucy deconvolution in double precision (the published

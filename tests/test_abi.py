@@ -155,3 +155,15 @@ def test_reuse_rl_and_batched_plan_entries_without_gpu(fclib):
     assert L.fc_rl_deconvolve_device(None, None, fc._iarr([64, 64, 32]), None, fc._iarr([5, 5, 5]), 3, 0, None, 0,
                                      None) == fc.FC_ERR_ARG
     assert L.fc_batched_last_plan(None) == -1
+    # subsampled kernel: only the image spectrum and the kernel's own-size
+    # spectrum, less than the plain path's padded kernel planes
+    sub = L.fc_conv3d_subsampled_workspace_bytes(fc._iarr([64, 64, 32]), fc._iarr([5, 5, 9]))
+    assert 0 < sub < L.fc_conv3d_workspace_bytes(fc._iarr([64, 64, 32]), fc._iarr([5, 5, 9]), 0)
+    assert L.fc_conv3d_subsampled_workspace_bytes(fc._iarr([64, 64, 32]), fc._iarr([5, 5, 33])) == 0
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    assert L.fc_conv3d_subsampled_device(None, None, fc._iarr([64, 64, 32]), None, fc._iarr([5, 5, 5]), None, 0,
+                                         None) == fc.FC_ERR_ARG
+    FP = ctypes.POINTER(ctypes.c_float)
+    k = np.ones((3, 3, 3), np.float32)
+    L.convolution3DfftCUDAInPlaceSaveMemory(None, fc._iarr([4, 4, 4]), k.ctypes.data_as(FP), fc._iarr([3, 3, 3]), 0)
+    assert L.fc_last_status() == fc.FC_ERR_ARG

@@ -159,3 +159,31 @@ def test_rl_oracle_conserves_flux_and_sharpens(orc):
     err = lambda a: np.linalg.norm(a - truth) / np.linalg.norm(truth)
     assert err(x) < 0.5 * err(y)
     assert np.allclose(orc.correlate_fp64(y, k), orc.conv_fp64(y, np.ascontiguousarray(k[::-1, ::-1, ::-1]), "centered"))
+
+
+def test_subsampled_oracle_index_map_and_known_answers(orc):
+    """The subsampled-kernel restatement (src/convolution3Dfft.cu:65-125):
+    the nearest-neighbour index map, r = 1 reading every kernel frequency once
+    (the odd-index negation is then a half-period shift on even axes), and a
+    1x1x1 kernel scaling the image."""
+    assert list(orc.subsampled_index(64, 64, 64)) == list(range(64))
+    assert orc.subsampled_index(512, 31, 257)[-1] == 16  # (kx+1)/2: one past the 16 stored columns
+    assert orc.subsampled_index(128, 63, 128)[-1] == 0  # 63 mod 63: the index wraps at the top
+    idx = orc.subsampled_index(100, 13, 100)
+    assert idx.min() >= 0 and idx.max() < 13 and np.all(np.diff(idx[:95]) >= 0)
+    rng = np.random.default_rng(2)
+    im = rng.random((8, 12, 16))
+    k = rng.random((8, 12, 16))
+    unshifted = np.fft.irfftn(np.fft.rfftn(im) * np.fft.rfftn(k), s=im.shape, axes=(0, 1, 2))
+    expect = np.roll(unshifted, (4, 6, 8), axis=(0, 1, 2))
+    assert np.max(np.abs(orc.subsampled_fp64(im, k) - expect)) <= 1e-12 * np.abs(expect).max()
+    assert np.max(np.abs(orc.subsampled_fp64(im, np.full((1, 1, 1), 2.0)) - 2 * im)) <= 1e-12
+    # odd kx: the x Nyquist reads the Hermitian mirror of the stored half spectrum
+    kk = rng.random((3, 5, 7))
+    A = orc.subsampled_coefficients(kk, (6, 10, 28))
+    full = np.fft.fftn(kk)
+    assert orc.subsampled_index(28, 7, 15)[-1] == 4  # past the 4 stored columns of kx = 7
+    iz, iy = orc.subsampled_index(6, 3, 6), orc.subsampled_index(10, 5, 10)
+    sign = np.where((iz[:, None] + iy[None, :] + 4) % 2 == 1, -1, 1)
+    mirror = np.conj(full[(-iz) % 3][:, (-iy) % 5, 3])
+    assert np.allclose(A[:, :, -1], sign * mirror, rtol=1e-12, atol=1e-12)
