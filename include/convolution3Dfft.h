@@ -63,10 +63,11 @@ FUNCTION_PREFIX void convolution3DfftCUDAInPlace(imageType* im, int* imDim, imag
  * kernel is transformed at its own size (no padding, no centring) and each
  * image frequency takes the nearest kernel frequency, (int)(r*f + 0.5) mod k
  * per axis with r = k/n, negated where the three kernel indices sum to an odd
- * number.  An approximation of the convolution (the reference states 2 %
- * maximum relative error for images larger than 5x the kernel); for an odd kx
- * the x index (kx+1)/2 takes the Hermitian mirror of the stored half spectrum
- * (the reference reads past its row there). */
+ * number (the phase of a shift by k/2: for an odd kernel edge the result
+ * lies half a voxel off the centred convolution along that axis).  An
+ * approximation of the convolution; for an odd kx the x index (kx+1)/2 takes
+ * the Hermitian mirror of the stored half spectrum (the reference reads past
+ * its row there). */
 FUNCTION_PREFIX void convolution3DfftCUDAInPlaceSaveMemory(imageType* im, int* imDim, imageType* kernel,
                                                            int* kernelDim, int devCUDA);
 
