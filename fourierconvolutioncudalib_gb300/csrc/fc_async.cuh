@@ -40,6 +40,18 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                : "memory");
 }
 
+// global -> shared tile copy through a tensor map (TMA, tile mode): the box
+// at element coordinates (x, y, z) of a 3-D map.  dst 128-byte aligned; x *
+// element size a multiple of 16 bytes; elements outside the map's extents
+// arrive as zeros (and count towards the barrier's bytes).
+__device__ __forceinline__ void tensor_load_3d(void* dst, const void* tmap, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_addr(dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ bool bar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(

@@ -12,6 +12,8 @@
 #ifndef FC_ZCONV_MIN_BLOCKS
 #define FC_ZCONV_MIN_BLOCKS 2
 #endif
+#include <cuda.h>
+
 #include "fc_async.cuh"
 #include "fc_fast.cuh"
 #include "fc_fast_sizes.h"
@@ -103,15 +105,34 @@ using ZTile = ColGeomB<N, 16>;
 // chain and its inverse the forward chain (either pairing hands the spectrum
 // over in registers; this one measured 0.4-2 % faster on GB300)
 constexpr bool kZRev = true;
+// z rows per tensor-map box of the image stage: the largest divisor of N of at
+// most 256 (a box dimension is at most 256, and equal boxes cover N exactly)
+constexpr int zbox_rows(int n) {
+  int nb = (n + 255) / 256;
+  while (n % nb) ++nb;
+  return n / nb;
+}
 template <int N>
 struct ZGeom {
-  // exchange tile, stash, image stage buffer (float2 elements); the stash
-  // starts on a 16-byte boundary (the exchange tile has N*B + N*B/16 entries,
-  // odd for some lengths) so that the stage buffer after it, the target of
-  // 16-byte cp.async copies, is 16-byte aligned too
+  // exchange tile, stash, image stage buffer, mbarrier (float2 elements); the
+  // stash starts on a 16-byte boundary (the exchange tile has N*B + N*B/16
+  // entries, odd for some lengths), and the stage buffer, the target of the
+  // tensor-map copy (or of the 16-byte cp.async copies), on a 128-byte one
   static constexpr int XCH = (ZTile<N>::SMEM + 1) & ~1;
+  static constexpr int STAGE_OFF = (XCH + ZTile<N>::THREADS * kVals + 15) & ~15;
   static constexpr int STAGE = N * ZTile<N>::B;
-  static constexpr int SMEM_BYTES = (XCH + ZTile<N>::THREADS * kVals + STAGE) * (int)sizeof(float2);
+  static constexpr int BAR_OFF = STAGE_OFF + STAGE;
+  static constexpr int SMEM_BYTES = (BAR_OFF + 2) * (int)sizeof(float2);
+  static constexpr int ZBOX = zbox_rows(N);
+  static constexpr int NBOX = N / ZBOX;
+  static constexpr unsigned STAGE_BYTES = (unsigned)STAGE * sizeof(float2);
+  static_assert(ZBOX <= 256 && ZBOX * NBOX == N, "tensor-map boxes must tile the column");
+  // the tensor-map stage is used for one box of 16 columns (z lengths up to
+  // 256); a stage of two 8-column boxes (z = 500) raised a GPU exception on its
+  // first run, with no cause found in its addresses, sizes or barrier count,
+  // so longer columns keep the cp.async stage
+  static constexpr bool TMA_OK = NBOX == 1 && ZTile<N>::B == 16;
+  static_assert(ZTile<N>::B * sizeof(float2) % 16 == 0, "box rows must be multiples of 16 bytes");
   // resident CTAs requested from the register allocator (256 threads: 2 -> <= 128 registers)
   static constexpr int MIN_BLOCKS =
       ZTile<N>::THREADS <= 256 ? FC_ZCONV_MIN_BLOCKS * (256 / ZTile<N>::THREADS) : 1;
@@ -119,12 +140,17 @@ struct ZGeom {
 
 // fused z pass body: tile (bx, ky); stash holds nstash >= THREADS slots per value index;
 // stage (optional) holds N*B float2 for the prefetched image tile
+// With `bar`, the stage was filled by a tensor-map copy on that mbarrier
+// (issued by the caller); the wait is bounded and a timeout ends the tile
+// (counted in g_zstage_timeouts).
+static __device__ unsigned int g_zstage_timeouts;
+
 template <int N, bool CONJ, int TCM = tc::kNone, class G = ColGeom<N>>
 __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch,
                                            int ny, int ncols, int kplanes, int hz, float scale,
                                            const float2* __restrict__ W, int bx, int ky, int tid, float2* sm,
                                            float2* stash, int nstash, const TcCtx& tcx = TcCtx{nullptr, nullptr},
-                                           float2* stage = nullptr) {
+                                           float2* stage = nullptr, uint64_t* bar = nullptr) {
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, kZRev>(), RF = last_radix<N, !kZRev>();
   const int c = tid % B;
@@ -134,7 +160,7 @@ __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2*
   const bool ok = col < ncols && t < G::T;
   const long long zs = (long long)ny * pitch;
   float2* base = S + (long long)ky * pitch + col;
-  if (stage) {
+  if (stage && !bar) {
     // 16-byte pieces (two columns) of the N x B image tile; pieces starting at
     // or beyond ncols are skipped (the row pitch covers the second column)
     const float2* src0 = S + (long long)ky * pitch + col0;
@@ -157,7 +183,13 @@ __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2*
   fft<N, false, TCM, kZRev>(v, lay, t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) stash[q * nstash + tid] = v[q];
-  if (stage) {
+  if (bar) {
+    const bool ready = async::bar_wait(bar, 0);
+    if (!__syncthreads_and(ready)) {
+      if (tid == 0) atomicAdd(&g_zstage_timeouts, 1u);
+      return;
+    }
+  } else if (stage) {
     async::wait_all();
     __syncthreads();
   }
@@ -188,17 +220,51 @@ __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2*
   }
 }
 
+// tmap: the spectrum as a 3-D tensor map (x: ncols columns, y: ny rows, z: N
+// planes; 8-byte elements, box B x 1 x N) when use_tma and ZGeom::TMA_OK,
+// else the image tile is staged with cp.async.  A stage that is not 128-byte
+// aligned also takes the cp.async path.
 template <int N, bool CONJ>
 __global__ void __launch_bounds__(ZTile<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zconv(
     float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
-    float scale, const float2* __restrict__ W) {
+    float scale, const float2* __restrict__ W, const __grid_constant__ CUtensorMap tmap, int use_tma) {
   using G = ZTile<N>;
-  extern __shared__ __align__(16) float2 zsm[];
-  float2* stash = zsm + ZGeom<N>::XCH;
-  float2* stage = stash + G::THREADS * kVals;  // THREADS * kVals is even: 16-byte aligned
+  using Z = ZGeom<N>;
+  extern __shared__ __align__(128) float2 zsm[];
+  float2* stash = zsm + Z::XCH;
+  float2* stage = zsm + Z::STAGE_OFF;
+  uint64_t* bar = nullptr;
+  if (Z::TMA_OK && use_tma && (async::smem_addr(stage) & 127u) == 0) {
+    bar = reinterpret_cast<uint64_t*>(zsm + Z::BAR_OFF);
+    if (threadIdx.x == 0) {
+      async::bar_init(bar, 1);
+      async::bar_init_fence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      async::bar_expect(bar, Z::STAGE_BYTES);
+      async::tensor_load_3d(stage, &tmap, (int)blockIdx.x * G::B, (int)blockIdx.y, 0, bar);
+    }
+  }
   body_zconv<N, CONJ, tc::kNone, G>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, W, (int)blockIdx.x,
                                     (int)blockIdx.y, (int)threadIdx.x, zsm, stash, G::THREADS,
-                                    TcCtx{nullptr, nullptr}, stage);
+                                    TcCtx{nullptr, nullptr}, stage, bar);
+}
+
+// Host: encode the tensor map of k_zconv's image stage for a spectrum of ncols
+// columns (row pitch `pitch` float2), ny rows and n planes; false when the
+// driver entry point is missing or the layout breaks a tensor-map rule.
+bool zstage_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int n, int box_cols,
+                       int box_rows);
+// Host: number of expired stage waits in this translation unit's kernels, cleared
+static inline unsigned int zstage_take_timeouts_tu() {
+  unsigned int v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_zstage_timeouts, sizeof(v)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (v) cudaMemcpyToSymbol(g_zstage_timeouts, &zero, sizeof(zero));
+  return v;
 }
 
 template <int N>

@@ -3,8 +3,11 @@
 // (templates in fc_fast_cols.cuh).
 #include "fc_fast_cols.cuh"
 
+#include <cstring>
+
 namespace fc {
 namespace fast {
+bool zstage_use_tma();
 // opt in to more than 48 KiB of dynamic shared memory where a kernel needs it
 template <class K>
 static cudaError_t set_dyn_smem(K kernel, int bytes) {
@@ -24,7 +27,12 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
     dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                   \
     const cudaError_t e = set_dyn_smem(k_zconv<n_, CONJ>, sm);                                                  \
     if (e != cudaSuccess) return e;                                                                             \
-    k_zconv<n_, CONJ><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W);        \
+    CUtensorMap map;                                                                                            \
+    std::memset(&map, 0, sizeof(map));                                                                          \
+    const int tma = ZGeom<n_>::TMA_OK && zstage_use_tma() &&                                                    \
+                    zstage_tensor_map(&map, S, pitch, ny, ncols, n_, G::B, ZGeom<n_>::ZBOX);                    \
+    k_zconv<n_, CONJ><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W, map,    \
+                                                    tma);                                                       \
     return cudaGetLastError();                                                                                  \
   }
     FC_COL_SIZES(FC_CASE)
@@ -39,6 +47,8 @@ cudaError_t fast_zconv_conj(float2* S, const float2* KXY, long long pitch, int n
                             float scale, const FcAxis& az, cudaStream_t st) {
   return fast::zconv_launch<true>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az, st);
 }
+
+unsigned int zadj_take_timeouts() { return fast::zstage_take_timeouts_tu(); }
 
 cudaError_t fast_zcorr(const float2* X, const float2* G_, float2* out, long long pitch, int ny, int ncols, int kz,
                        int hz, float scale, const FcAxis& az, cudaStream_t st) {

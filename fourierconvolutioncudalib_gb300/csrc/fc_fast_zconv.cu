@@ -3,8 +3,48 @@
 // conjugate-kernel and kernel-gradient variants are in fc_fast_zadj.cu).
 #include "fc_fast_cols.cuh"
 
+#include <cudaTypedefs.h>
+
+#include <cstdlib>
+#include <cstring>
+
 namespace fc {
 namespace fast {
+
+bool zstage_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int n, int box_cols,
+                       int box_rows) {
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    cudaGetLastError();
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode || ((uintptr_t)S & 15) != 0 || (pitch * (long long)sizeof(float2)) % 16 != 0 || box_rows > 256 ||
+      box_cols > 256 || (box_cols * sizeof(float2)) % 16 != 0)
+    return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)ny, (cuuint64_t)n};
+  const cuuint64_t strides[2] = {(cuuint64_t)pitch * sizeof(float2), (cuuint64_t)pitch * sizeof(float2) * ny};
+  const cuuint32_t box[3] = {(cuuint32_t)box_cols, 1u, (cuuint32_t)box_rows};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<float2*>(S), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// FC_ZSTAGE_TMA=0 stages the fused z pass's image tile with cp.async instead
+// of the tensor-map copy
+bool zstage_use_tma() {
+  static const bool on = [] {
+    const char* e = std::getenv("FC_ZSTAGE_TMA");
+    return !e || std::atoi(e) != 0;
+  }();
+  return on;
+}
+
 // opt in to more than 48 KiB of dynamic shared memory where a kernel needs it
 template <class K>
 static cudaError_t set_dyn_smem(K kernel, int bytes) {
@@ -24,7 +64,12 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
     dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                   \
     const cudaError_t e = set_dyn_smem(k_zconv<n_, CONJ>, sm);                                                  \
     if (e != cudaSuccess) return e;                                                                             \
-    k_zconv<n_, CONJ><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W);        \
+    CUtensorMap map;                                                                                            \
+    std::memset(&map, 0, sizeof(map));                                                                          \
+    const int tma = ZGeom<n_>::TMA_OK && zstage_use_tma() &&                                                    \
+                    zstage_tensor_map(&map, S, pitch, ny, ncols, n_, G::B, ZGeom<n_>::ZBOX);                    \
+    k_zconv<n_, CONJ><<<grid, G::THREADS, sm, st>>>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W, map,    \
+                                                    tma);                                                       \
     return cudaGetLastError();                                                                                  \
   }
     FC_COL_SIZES(FC_CASE)
@@ -34,6 +79,8 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
   }
 }
 }  // namespace fast
+
+unsigned int zconv_take_timeouts() { return fast::zstage_take_timeouts_tu(); }
 
 cudaError_t fast_zconv_conj(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
                             float scale, const FcAxis& az, cudaStream_t st);

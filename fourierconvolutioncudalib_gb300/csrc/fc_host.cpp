@@ -1010,6 +1010,12 @@ static bool host_buffer_pinned(const void* p) {
   return a.type == cudaMemoryTypeHost;
 }
 
+// bounded device waits that expired since the last check (pipelined x passes,
+// tensor-map stage of the fused z passes)
+static unsigned int take_device_timeouts() {
+  return pipe_take_timeouts() + zconv_take_timeouts() + zadj_take_timeouts();
+}
+
 // Host-pointer convolution used by the three reference-compatible entry points.
 static void host_conv(const float* im, float* out, int nx, int ny, int nz, const float* kernel, int kx, int ky,
                       int kz, bool dense, int dev, bool allow_direct = false, bool subsampled = false) {
@@ -1039,7 +1045,7 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
       run(im, out);
     }
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-    if (pipe_take_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in a pipelined pass");
+    if (take_device_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in an asynchronous copy");
     return;
   }
   grow((void**)&c.d_img, &c.img_cap, nimg, "cudaMalloc(image)");
@@ -1047,7 +1053,7 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
   run(c.d_img, c.d_img);
   cuda_check(cudaMemcpyAsync(out, c.d_img, nimg, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync(result D2H)");
   cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-  if (pipe_take_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in a pipelined pass");
+  if (take_device_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in an asynchronous copy");
 }
 
 template <class F>

@@ -121,6 +121,10 @@ cudaError_t pipe_x_r2c_dense(const float* in, long long in_pitch, float2* out, l
 cudaError_t pipe_x_c2r(const float2* in, long long in_pitch, float* out, long long out_pitch, long long nrows,
                        const FcAxis& ax, cudaStream_t st);
 unsigned int pipe_take_timeouts();
+// expired waits of the fused z passes' tensor-map stage copies (plain and
+// conjugate-kernel kernels), returned and cleared
+unsigned int zconv_take_timeouts();
+unsigned int zadj_take_timeouts();
 // in-place y pass on wide tiles (fast::ColGeomWide); covers the column
 // lengths plus FC_WIDE_ONLY_SIZES
 bool fast_cols_wide_supported(int n);
