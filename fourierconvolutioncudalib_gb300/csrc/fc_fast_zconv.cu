@@ -11,8 +11,9 @@
 namespace fc {
 namespace fast {
 
-bool zstage_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int n, int box_cols,
-                       int box_rows) {
+// the driver's tensor-map encoder, looked up once (first from zstage_prepare,
+// which the host calls when it creates a device context, outside any capture)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -23,6 +24,12 @@ bool zstage_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int n
     cudaGetLastError();
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }();
+  return encode;
+}
+
+bool zstage_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int n, int box_cols,
+                       int box_rows) {
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
   if (!encode || ((uintptr_t)S & 15) != 0 || (pitch * (long long)sizeof(float2)) % 16 != 0 || box_rows > 256 ||
       box_cols > 256 || (box_cols * sizeof(float2)) % 16 != 0)
     return false;
@@ -81,6 +88,8 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
 }  // namespace fast
 
 unsigned int zconv_take_timeouts() { return fast::zstage_take_timeouts_tu(); }
+
+void zstage_prepare() { (void)fast::tensor_map_encoder(); }
 
 cudaError_t fast_zconv_conj(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,
                             float scale, const FcAxis& az, cudaStream_t st);

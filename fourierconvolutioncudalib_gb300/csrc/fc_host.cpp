@@ -164,6 +164,7 @@ static DevCtx& ctx_for(int dev) {
   c->dev = dev;
   DevCtx& ref = *c;
   g_ctx[dev] = std::move(c);
+  zstage_prepare();  // a driver entry-point lookup: here, not inside a later stream capture
   return ref;
 }
 

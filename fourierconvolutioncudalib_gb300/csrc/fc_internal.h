@@ -125,6 +125,9 @@ unsigned int pipe_take_timeouts();
 // conjugate-kernel kernels), returned and cleared
 unsigned int zconv_take_timeouts();
 unsigned int zadj_take_timeouts();
+// resolve the tensor-map encoder of the fused z pass's stage copy (host; call
+// outside stream capture, e.g. when a device context is created)
+void zstage_prepare();
 // in-place y pass on wide tiles (fast::ColGeomWide); covers the column
 // lengths plus FC_WIDE_ONLY_SIZES
 bool fast_cols_wide_supported(int n);
