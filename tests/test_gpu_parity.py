@@ -105,6 +105,8 @@ def test_c1_vs_cufft_sequence(cuda, orc, kernels):
     ((250, 48, 64), (9, 5, 7)),       # z lengths whose fused-z tiles are 8 and 4 columns wide
     ((500, 20, 30), (7, 3, 5)),
     ((900, 24, 20), (11, 5, 3)),
+    ((16, 64, 48), (3, 7, 5)),        # kernel rows exactly fill the kernel y pass's first-stage stride (4)
+    ((20, 64, 40), (3, 15, 5)),       # kernel rows beyond that stride: full first stage
 ])
 def test_shapes_vs_fp64(cuda, orc, kernels, host_io, shape, kshape):
     rng = np.random.default_rng(sum(shape) + sum(kshape))
