@@ -1,8 +1,8 @@
 // The reference's convolution3DfftCUDAInPlace restated on cuFFT -- a timing
 // baseline and parity harness only, never part of the product library.
 //
-// The reference sources cannot be built on the GPU host (they are not there),
-// so this file re-expresses the same host and device sequence of
+// The reference sources are not part of this repository, so this file
+// re-expresses the same host and device sequence of
 // src/convolution3Dfft.cu:399-578 in its own code:
 //   host pad of the image into R2C rows (:495-510), H2D (:512-515),
 //   fftShiftKernel scatter (:442-461) + per-row D2D copies (:474-486),

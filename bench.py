@@ -21,8 +21,8 @@ Line fields (one JSON line from rank 0):
   ref_cufft the reference's device sequence (cuFFT R2C x2, modulate, C2R)
             on the same GPU, for comparison.
 `--impl reference` times the reference algorithm on the host instead (the
-oracle's float32 port; the reference library itself needs cuFFT on a GPU and
-its sources are not on the GPU host).
+oracle's float32 port; the reference library's own sources are not part of
+this repository, so it is not built where the benchmark runs).
 """
 from __future__ import annotations
 

@@ -10,7 +10,7 @@ set -euo pipefail
 REF=${REF:-/root/reference}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
-# absent reference tree (e.g. on the GPU host): nothing to build, not an error
+# absent reference tree (a machine without the reference sources): nothing to build, not an error
 [ -d "$REF/src" ] || { echo "reference sources not present: skipped" >&2; exit 0; }
 mkdir -p "$OUT"
 NVCC=${NVCC:-nvcc}

@@ -1,7 +1,7 @@
 """The N>1 path of bench.py on CPU: two gloo ranks on 127.0.0.1.
 
-bench.py runs one process per GPU under torchrun; on the GPU host NCCL
-carries the max-over-ranks reduction.  Here the same code runs with the gloo
+bench.py runs one process per GPU under torchrun; with GPUs NCCL carries
+the max-over-ranks reduction.  Here the same code runs with the gloo
 backend (FC_BENCH_BACKEND=gloo): the rank helpers reduce to the maximum and
 the reference arm prints exactly one JSON line, from rank 0, with the world
 size as n_gpus, while rank 1 exits 0 without work.
