@@ -256,15 +256,14 @@ __global__ void __launch_bounds__(ZTile<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zco
 // driver entry point is missing or the layout breaks a tensor-map rule.
 bool zstage_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int n, int box_cols,
                        int box_rows);
-// Host: number of expired stage waits in this translation unit's kernels, cleared
-static inline unsigned int zstage_take_timeouts_tu() {
-  unsigned int v = 0, zero = 0;
-  if (cudaMemcpyFromSymbol(&v, g_zstage_timeouts, sizeof(v)) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  if (v) cudaMemcpyToSymbol(g_zstage_timeouts, &zero, sizeof(zero));
-  return v;
+// Host: enqueue a read of this translation unit's count of expired stage
+// waits into dst (page-locked host memory) on st; clear the count
+static inline cudaError_t zstage_timeouts_read_async_tu(unsigned int* dst, cudaStream_t st) {
+  return cudaMemcpyFromSymbolAsync(dst, g_zstage_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
+}
+static inline void zstage_timeouts_clear_tu() {
+  const unsigned int zero = 0;
+  cudaMemcpyToSymbol(g_zstage_timeouts, &zero, sizeof(zero));
 }
 
 template <int N>

@@ -150,14 +150,13 @@ cudaError_t pipe_x_c2r(const float2* in, long long in_pitch, float* out, long lo
   }
 }
 
-unsigned int pipe_take_timeouts() {
-  unsigned int n = 0, zero = 0;
-  if (cudaMemcpyFromSymbol(&n, fast::g_pipe_timeouts, sizeof(n)) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  if (n) cudaMemcpyToSymbol(fast::g_pipe_timeouts, &zero, sizeof(zero));
-  return n;
+cudaError_t pipe_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
+  return cudaMemcpyFromSymbolAsync(dst, fast::g_pipe_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
+}
+
+void pipe_timeouts_clear() {
+  const unsigned int zero = 0;
+  cudaMemcpyToSymbol(fast::g_pipe_timeouts, &zero, sizeof(zero));
 }
 
 }  // namespace fc

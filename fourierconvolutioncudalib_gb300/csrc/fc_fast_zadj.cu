@@ -48,7 +48,10 @@ cudaError_t fast_zconv_conj(float2* S, const float2* KXY, long long pitch, int n
   return fast::zconv_launch<true>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az, st);
 }
 
-unsigned int zadj_take_timeouts() { return fast::zstage_take_timeouts_tu(); }
+cudaError_t zadj_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
+  return fast::zstage_timeouts_read_async_tu(dst, st);
+}
+void zadj_timeouts_clear() { fast::zstage_timeouts_clear_tu(); }
 
 cudaError_t fast_zcorr(const float2* X, const float2* G_, float2* out, long long pitch, int ny, int ncols, int kz,
                        int hz, float scale, const FcAxis& az, cudaStream_t st) {

@@ -87,7 +87,10 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
 }
 }  // namespace fast
 
-unsigned int zconv_take_timeouts() { return fast::zstage_take_timeouts_tu(); }
+cudaError_t zconv_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
+  return fast::zstage_timeouts_read_async_tu(dst, st);
+}
+void zconv_timeouts_clear() { fast::zstage_timeouts_clear_tu(); }
 
 void zstage_prepare() { (void)fast::tensor_map_encoder(); }
 

@@ -128,6 +128,9 @@ struct DevCtx {
   // streams and events of the view-concurrent batched schedule (created on first use)
   std::vector<cudaStream_t> bstreams;
   std::vector<cudaEvent_t> bevents;
+  // page-locked counts of expired bounded device waits, read on the stream
+  // before a synchronous entry's final synchronisation (created on first use)
+  unsigned int* h_timeouts = nullptr;
 };
 
 // The kernel-spectrum passes depend only on the kernel, so they can run on a
@@ -1011,10 +1014,21 @@ static bool host_buffer_pinned(const void* p) {
   return a.type == cudaMemoryTypeHost;
 }
 
-// bounded device waits that expired since the last check (pipelined x passes,
-// tensor-map stage of the fused z passes)
-static unsigned int take_device_timeouts() {
-  return pipe_take_timeouts() + zconv_take_timeouts() + zadj_take_timeouts();
+// Bounded device waits (pipelined x passes, tensor-map stage of the fused z
+// passes): enqueue reads of their expiry counts on st, to be checked after
+// the stream's synchronisation by check_device_timeouts.
+static void enqueue_timeout_reads(DevCtx& c, cudaStream_t st) {
+  if (!c.h_timeouts) cuda_check(cudaHostAlloc((void**)&c.h_timeouts, 4 * sizeof(unsigned int), 0), "cudaHostAlloc");
+  cuda_check(pipe_timeouts_read_async(c.h_timeouts, st), "timeout count read");
+  cuda_check(zconv_timeouts_read_async(c.h_timeouts + 1, st), "timeout count read");
+  cuda_check(zadj_timeouts_read_async(c.h_timeouts + 2, st), "timeout count read");
+}
+static void check_device_timeouts(DevCtx& c) {
+  if (!(c.h_timeouts[0] | c.h_timeouts[1] | c.h_timeouts[2])) return;
+  pipe_timeouts_clear();
+  zconv_timeouts_clear();
+  zadj_timeouts_clear();
+  FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in an asynchronous copy");
 }
 
 // Host-pointer convolution used by the three reference-compatible entry points.
@@ -1045,16 +1059,18 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
       HostSrcScope hs(true);
       run(im, out);
     }
+    enqueue_timeout_reads(c, st);
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-    if (take_device_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in an asynchronous copy");
+    check_device_timeouts(c);
     return;
   }
   grow((void**)&c.d_img, &c.img_cap, nimg, "cudaMalloc(image)");
   cuda_check(cudaMemcpyAsync(c.d_img, im, nimg, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(image H2D)");
   run(c.d_img, c.d_img);
   cuda_check(cudaMemcpyAsync(out, c.d_img, nimg, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync(result D2H)");
+  enqueue_timeout_reads(c, st);
   cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-  if (take_device_timeouts()) FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in an asynchronous copy");
+  check_device_timeouts(c);
 }
 
 template <class F>
@@ -1874,6 +1890,7 @@ int fc_release_device(int devCUDA) {
     if (c->ev_done) cudaEventDestroy(c->ev_done);
     for (cudaStream_t s2 : c->bstreams) cudaStreamDestroy(s2);
     for (cudaEvent_t e2 : c->bevents) cudaEventDestroy(e2);
+    if (c->h_timeouts) cudaFreeHost(c->h_timeouts);
     cudaSetDevice(prev);
   });
 }

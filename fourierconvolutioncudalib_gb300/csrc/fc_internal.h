@@ -114,17 +114,21 @@ cudaError_t launch_stage_twiddles(float2* W, int n, cudaStream_t st);
 
 // Pipelined x passes (fc_fast_pipe.cu): persistent CTAs with bulk
 // asynchronous tile copies.  in must be device memory, 16-byte aligned, with
-// rows of a multiple of 16 bytes.  pipe_take_timeouts() returns and clears the
-// number of bounded waits that expired.
+// rows of a multiple of 16 bytes.  pipe_timeouts_read_async() enqueues a read
+// of the number of bounded waits that expired into page-locked host memory;
+// pipe_timeouts_clear() resets it.
 cudaError_t pipe_x_r2c_dense(const float* in, long long in_pitch, float2* out, long long out_pitch, long long nrows,
                              const FcAxis& ax, cudaStream_t st);
 cudaError_t pipe_x_c2r(const float2* in, long long in_pitch, float* out, long long out_pitch, long long nrows,
                        const FcAxis& ax, cudaStream_t st);
-unsigned int pipe_take_timeouts();
-// expired waits of the fused z passes' tensor-map stage copies (plain and
-// conjugate-kernel kernels), returned and cleared
-unsigned int zconv_take_timeouts();
-unsigned int zadj_take_timeouts();
+cudaError_t pipe_timeouts_read_async(unsigned int* dst, cudaStream_t st);
+void pipe_timeouts_clear();
+// the same for the fused z passes' tensor-map stage copies (plain and
+// conjugate-kernel kernels)
+cudaError_t zconv_timeouts_read_async(unsigned int* dst, cudaStream_t st);
+void zconv_timeouts_clear();
+cudaError_t zadj_timeouts_read_async(unsigned int* dst, cudaStream_t st);
+void zadj_timeouts_clear();
 // resolve the tensor-map encoder of the fused z pass's stage copy (host; call
 // outside stream capture, e.g. when a device context is created)
 void zstage_prepare();
