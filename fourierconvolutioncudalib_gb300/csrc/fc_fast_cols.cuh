@@ -138,13 +138,15 @@ struct ZGeom {
       ZTile<N>::THREADS <= 256 ? FC_ZCONV_MIN_BLOCKS * (256 / ZTile<N>::THREADS) : 1;
 };
 
-// fused z pass body: tile (bx, ky); stash holds nstash >= THREADS slots per value index;
-// stage (optional) holds N*B float2 for the prefetched image tile
-// With `bar`, the stage was filled by a tensor-map copy on that mbarrier
-// (issued by the caller); the wait is bounded and a timeout ends the tile
-// (counted in g_zstage_timeouts).
+// expired waits of the fused z pass's tensor-map stage (one count per
+// translation unit that instantiates k_zconv)
 static __device__ unsigned int g_zstage_timeouts;
 
+// fused z pass body: tile (bx, ky); stash holds nstash >= THREADS slots per value index;
+// stage (optional) holds N*B float2 for the prefetched image tile.  With
+// `bar`, the stage was filled by a tensor-map copy on that mbarrier (issued by
+// the caller); the wait is bounded and a timeout ends the tile (counted in
+// g_zstage_timeouts).  Without it the body stages the tile with cp.async.
 template <int N, bool CONJ, int TCM = tc::kNone, class G = ColGeom<N>>
 __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch,
                                            int ny, int ncols, int kplanes, int hz, float scale,
