@@ -187,3 +187,36 @@ def test_subsampled_oracle_index_map_and_known_answers(orc):
     sign = np.where((iz[:, None] + iy[None, :] + 4) % 2 == 1, -1, 1)
     mirror = np.conj(full[(-iz) % 3][:, (-iy) % 5, 3])
     assert np.allclose(A[:, :, -1], sign * mirror, rtol=1e-12, atol=1e-12)
+
+
+def test_subsampled_coefficients_match_the_reference_loop(orc):
+    """The vectorised coefficient map equals a literal restatement of the
+    reference's per-element loop (src/convolution3Dfft.cu:68-117): flat index
+    i over the half spectrum, dimension 2 fastest, the nearest-neighbour
+    indices in float32 with the multiply-add rounded once, the packed
+    half-spectrum read k2 + aux*(k1 + kd1*k0), and the parity negation.  Even
+    kx keeps every read inside its row (odd kx is covered by the mirror test)."""
+    rng = np.random.default_rng(5)
+    for shape, kshape in (((6, 10, 12), (3, 5, 4)), ((7, 9, 16), (5, 3, 6)), ((4, 4, 8), (4, 4, 8))):
+        kernel = rng.random(kshape)
+        imd = shape        # (imDim_0, imDim_1, imDim_2): dimension 2 fastest
+        kd = kshape
+        packed = np.fft.rfftn(kernel).ravel()  # [kd0][kd1][kd2/2+1]
+        r = [np.float32(np.float32(kd[a]) / np.float32(imd[a])) for a in range(3)]
+
+        def near(ra, f, k):
+            return int(np.float32(np.float64(ra) * f + 0.5)) % k
+
+        aux = 1 + imd[2] // 2
+        n = imd[0] * imd[1] * aux
+        loop = np.empty(n, np.complex128)
+        for i in range(n):
+            k2 = i % aux
+            q = (i - k2) // aux
+            k1 = q % imd[1]
+            k0 = (q - k1) // imd[1]
+            k2, k1, k0 = near(r[2], k2, kd[2]), near(r[1], k1, kd[1]), near(r[0], k0, kd[0])
+            a = packed[k2 + (1 + kd[2] // 2) * (k1 + kd[1] * k0)]
+            loop[i] = -a if (k0 + k1 + k2) % 2 == 1 else a
+        got = orc.subsampled_coefficients(kernel, shape).ravel()
+        assert np.allclose(got, loop, rtol=0, atol=1e-12 * np.abs(loop).max()), (shape, kshape)
