@@ -640,9 +640,28 @@ def time_cpu_baseline(im_np, k_np):
         orc.reference_path_fp32(im_np, k_np, "centered", workers=cores)
         ts.append(time.perf_counter() - t)
     s = statistics.mean(ts)
-    return {"value": im_np.size / s / 1e9, "unit": "Gvoxel/s", "cores": cores, "kind": "port",
-            "sample": f"{n} full-volume convolutions (after 1 warm-up): the reference algorithm in float32 on the "
-                      f"host, scipy.fft transforms on {cores} threads"}
+    out = {"value": im_np.size / s / 1e9, "unit": "Gvoxel/s", "cores": cores, "kind": "port",
+           "sample": f"{n} full-volume convolutions (after 1 warm-up): the reference algorithm in float32 on the "
+                     f"host, scipy.fft transforms on {cores} threads"}
+    # the reference test suite's CPU convolution (tests/test_algorithms.hpp:10-58: direct spatial sum, float
+    # accumulator, periodic here) on output crops at the volume's centre, all cores and one thread; the
+    # full-volume time is extrapolated from the crop
+    try:
+        ds = {}
+        for label, crop, threads in (("all_cores", (16, 32, 32), cores), ("one_thread", (4, 16, 16), 1)):
+            c0 = tuple((nn - cc) // 2 for nn, cc in zip(im_np.shape, crop))
+            t = time.perf_counter()
+            orc.convolve_direct_crop(im_np, k_np, c0, crop, threads=threads)
+            dt = time.perf_counter() - t
+            nv = int(np.prod(crop))
+            ds[label] = {"value": nv / dt / 1e9, "unit": "Gvoxel/s", "cores": threads,
+                         "crop_zyx": list(crop), "seconds": dt,
+                         "full_volume_seconds_extrapolated": dt * im_np.size / nv}
+        ds["what"] = "direct spatial sum of the reference test suite's CPU convolution, on output crops"
+        out["direct_sum"] = ds
+    except Exception as e:  # the FFT-based baseline above stands on its own
+        out["direct_sum"] = {"unavailable": repr(e)[:200]}
+    return out
 
 
 def main():
