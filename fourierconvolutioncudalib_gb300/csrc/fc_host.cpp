@@ -2178,6 +2178,8 @@ int fc_conv3d_batched_device(int n_views, const float* const* d_images, float* c
     std::vector<Geom> gs;
     size_t need = 0;
     for (int v = 0; v < n_views; ++v) {
+      if (!d_images[v] || !d_outs[v] || !d_kernels[v])
+        FC_THROW(FC_ERR_ARG, "NULL image, output or kernel pointer of view " + std::to_string(v));
       const int* d = dims + 6 * v;
       gs.push_back(make_geom(d[0], d[1], d[2], d[3], d[4], d[5], false));
       need += plain_layout(gs.back(), compat).total;

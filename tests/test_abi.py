@@ -167,3 +167,35 @@ def test_reuse_rl_and_batched_plan_entries_without_gpu(fclib):
     k = np.ones((3, 3, 3), np.float32)
     L.convolution3DfftCUDAInPlaceSaveMemory(None, fc._iarr([4, 4, 4]), k.ctypes.data_as(FP), fc._iarr([3, 3, 3]), 0)
     assert L.fc_last_status() == fc.FC_ERR_ARG
+
+
+def test_other_entries_refuse_bad_arguments_without_gpu(fclib):
+    """The adjoint, batched, transform and placement entries check their
+    arguments on the host: bad shapes give a zero workspace size with
+    FC_ERR_ARG, and NULL pointers (including one view's pointer in a batch)
+    are refused before any device work."""
+    import fourierconvolutioncudalib_gb300 as fc
+
+    L = fc.lib()
+    I = fc._iarr
+    assert L.fc_conv3d_adjoint_workspace_bytes(I([64, 64, 32]), I([5, 5, 5]), 0) > 0
+    assert L.fc_conv3d_adjoint_workspace_bytes(I([64, 64, 32]), I([65, 5, 5]), 0) == 0
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    assert L.fc_fft3d_workspace_bytes(I([64, 64, 32])) > 0
+    assert L.fc_fft3d_workspace_bytes(I([0, 64, 32])) == 0
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    two = I([64, 64, 32, 5, 5, 5, 32, 32, 16, 3, 3, 3])
+    assert L.fc_conv3d_batched_workspace_bytes(2, two, 0) > L.fc_conv3d_batched_workspace_bytes(1, two, 0) > 0
+    assert L.fc_conv3d_batched_workspace_bytes(0, None, 0) == 0
+    assert L.fc_last_status() == fc.FC_ERR_ARG
+    assert L.fc_rfft3d_device(None, None, I([8, 8, 8]), None, 0, None) == fc.FC_ERR_ARG
+    assert L.fc_irfft3d_device(None, None, I([8, 8, 8]), None, 0, None) == fc.FC_ERR_ARG
+    assert L.fc_pad_shift_kernel_device(None, I([3, 3, 3]), I([8, 8, 8]), 0, None, None) == fc.FC_ERR_ARG
+    assert L.fc_conv3d_adjoint_device(None, None, None, None, None, I([8, 8, 8]), I([3, 3, 3]), 0, None, 0,
+                                      None) == fc.FC_ERR_ARG
+    P = ctypes.c_void_p
+    views = (P * 2)(P(4096), None)  # the second view's pointer is NULL
+    rc = L.fc_conv3d_batched_device(2, views, views, views, I([8, 8, 8, 3, 3, 3, 8, 8, 8, 3, 3, 3]), 0, None, 0,
+                                    None)
+    assert rc == fc.FC_ERR_ARG
+    assert "view 1" in L.fc_last_error().decode()
