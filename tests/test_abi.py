@@ -199,3 +199,18 @@ def test_other_entries_refuse_bad_arguments_without_gpu(fclib):
                                     None)
     assert rc == fc.FC_ERR_ARG
     assert "view 1" in L.fc_last_error().decode()
+
+
+def test_device_wrappers_refuse_host_tensors(fclib):
+    """The torch wrappers accept only contiguous float32 CUDA tensors and say
+    so before calling the library."""
+    torch = pytest.importorskip("torch")
+    import fourierconvolutioncudalib_gb300 as fc
+    from fourierconvolutioncudalib_gb300 import device as fcd
+
+    img = torch.zeros((8, 8, 8))
+    ker = torch.ones((3, 3, 3)) / 27
+    for call in (lambda: fcd.conv3d(img, ker), lambda: fcd.conv3d_subsampled(img, ker),
+                 lambda: fcd.rl_deconvolve(img, ker, 1), lambda: fcd.kernel_spectrum(ker, (8, 8, 8))):
+        with pytest.raises(fc.FcError, match="CUDA tensor"):
+            call()
