@@ -210,6 +210,15 @@ void fco_modulate_and_normalize(float* dst, const float* src, long long n, float
   }
 }
 
+/* src/convolution3Dfft.cu:68-70, :106-108: the kernel index read by image
+ * frequencies f = 0..m-1 of an axis of length n, for a kernel of length k:
+ * (int)(r*f + 0.5f) % k with r = (float)k / (float)n, the multiply-add rounded
+ * once (fmaf) as in the reference's contracted device expression. */
+void fco_subsampled_index(int n, int k, int m, int* out) {
+  const float r = (float)k / (float)n;
+  for (int f = 0; f < m; ++f) out[f] = ((int)fmaf(r, (float)f, 0.5f)) % k;
+}
+
 /* tests/test_utils.hpp:76-88: sqrt(sum (data-ref)^2) / n, accumulated in double */
 double fco_l2norm(const float* reference, const float* data, long long n) {
   double s = 0.0;

@@ -73,6 +73,8 @@ def lib() -> ctypes.CDLL:
         L.fco_l2norm_by_nvidia.restype = ctypes.c_double
         L.fco_l2norm_by_nvidia.argtypes = [_FP, _FP, ctypes.c_longlong]
         L.fco_max_threads.restype = _I
+        L.fco_subsampled_index.restype = None
+        L.fco_subsampled_index.argtypes = [_I, _I, _I, _IP]
         _lib = L
     return _lib
 
@@ -229,6 +231,14 @@ def subsampled_index(n: int, k: int, m: int) -> np.ndarray:
     f = np.arange(m, dtype=np.float64)
     v = (np.float64(r) * f + 0.5).astype(np.float32)
     return np.trunc(v).astype(np.int64) % k
+
+
+def subsampled_index_c(n: int, k: int, m: int) -> np.ndarray:
+    """subsampled_index restated in C with fmaf (fc_oracle.c), for cross-checking
+    the float64 emulation of the fused float32 multiply-add."""
+    out = np.empty(m, np.int32)
+    lib().fco_subsampled_index(int(n), int(k), int(m), out.ctypes.data_as(_IP))
+    return out
 
 
 def subsampled_coefficients(kernel: np.ndarray, image_shape_zyx: Sequence[int]) -> np.ndarray:

@@ -220,3 +220,22 @@ def test_subsampled_coefficients_match_the_reference_loop(orc):
             loop[i] = -a if (k0 + k1 + k2) % 2 == 1 else a
         got = orc.subsampled_coefficients(kernel, shape).ravel()
         assert np.allclose(got, loop, rtol=0, atol=1e-12 * np.abs(loop).max()), (shape, kshape)
+
+
+def test_subsampled_index_emulation_matches_fmaf(orc):
+    """The numpy index map (float64 multiply-add, one cast to float32) equals a C
+    restatement with fmaf (one rounding by definition) over every frequency of
+    a grid of axis and kernel lengths, including the ratios near ties."""
+    rng = np.random.default_rng(11)
+    ns = sorted(set([1, 2, 3, 7, 16, 31, 63, 64, 96, 100, 127, 128, 200, 250, 255, 256, 333, 384, 448, 500, 512,
+                     600, 720, 1000, 1024, 2048, 4096] + list(rng.integers(1, 4097, 40))))
+    checked = 0
+    for n in ns:
+        ks = sorted(set([1, 2, 3, n] + [k for k in (5, 7, 9, 15, 21, 31, 41, 63, 64, 127) if k <= n] +
+                        list(rng.integers(1, n + 1, 6))))
+        for k in ks:
+            a = orc.subsampled_index(int(n), int(k), int(n))
+            b = orc.subsampled_index_c(int(n), int(k), int(n))
+            assert np.array_equal(a, b), (n, k, np.nonzero(a != b)[0][:5])
+            checked += int(n)
+    assert checked > 100000
