@@ -150,12 +150,16 @@ __host__ __device__ constexpr int run_off(int m, int step) {
 // base + m NS (m < R) inside the NS*R-aligned block of the butterfly
 template <class L>
 __host__ __device__ constexpr bool lin_write(int NS, int R) {
-  return L::D == 0 || NS % L::D == 0 || (L::D % NS == 0 && ((NS * R) % L::D == 0 || L::D % (NS * R) == 0));
+  if (L::D == 0) return true;  // no padding: every run is linear
+  const int D = L::D ? L::D : 1;  // (not zero here; spelled so for the front end)
+  return NS % D == 0 || (D % NS == 0 && ((NS * R) % D == 0 || D % (NS * R) == 0));
 }
 // read run: j + m NB (any j)
 template <class L>
 __host__ __device__ constexpr bool lin_read(int NB) {
-  return L::D == 0 || NB % L::D == 0;
+  if (L::D == 0) return true;
+  const int D = L::D ? L::D : 1;  // (not zero here; spelled so for the front end)
+  return NB % D == 0;
 }
 
 // stage I of the forward chain (REV = false) or of the reversed chain (REV = true);
