@@ -214,3 +214,31 @@ def test_device_wrappers_refuse_host_tensors(fclib):
                  lambda: fcd.rl_deconvolve(img, ker, 1), lambda: fcd.kernel_spectrum(ker, (8, 8, 8))):
         with pytest.raises(fc.FcError, match="CUDA tensor"):
             call()
+
+
+def test_header_compiles_as_c_and_links_from_cpp(fclib, tmp_path):
+    """include/convolution3Dfft.h is usable from C (C99) and from C++, and a
+    C++ program that calls the reference entry points links against the
+    library by its JNA name (built, not run: running needs a GPU)."""
+    import shutil
+
+    import fourierconvolutioncudalib_gb300 as fc
+
+    gcc, gxx = shutil.which("gcc"), shutil.which("g++")
+    if not gcc or not gxx:
+        pytest.skip("no host C/C++ compiler")
+    inc = str(ROOT / "include")
+    c_src = tmp_path / "use.c"
+    c_src.write_text('#include "convolution3Dfft.h"\n'
+                     'int main(void) { int d[3] = {8, 8, 8}; float im[512], k[27];\n'
+                     '  convolution3DfftCUDAInPlace(im, d, k, d, 0); return fc_last_status(); }\n')
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", inc, "-c", str(c_src), "-o",
+                    str(tmp_path / "use.o")], check=True)
+    cpp_src = tmp_path / "use.cpp"
+    cpp_src.write_text('#include "convolution3Dfft.h"\n'
+                       'int main() { int d[3] = {8, 8, 8}; float* out = convolution3DfftCUDA(nullptr, d, nullptr, d, 0);\n'
+                       '  fc_free_result(out); return getNumDevicesCUDA() < 0; }\n')
+    lib = fc.library_path()
+    subprocess.run([gxx, "-std=c++11", "-Wall", "-Wextra", "-Werror", "-I", inc, str(cpp_src), "-L", str(lib.parent),
+                    "-lFourierConvolutionCUDALib", "-Wl,-rpath," + str(lib.parent), "-o", str(tmp_path / "use")],
+                   check=True)
