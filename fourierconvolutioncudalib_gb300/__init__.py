@@ -108,6 +108,9 @@ _SIGNATURES = {
     "fc_profile_read": (_I, [ctypes.c_char_p, _I, _FP, ctypes.POINTER(ctypes.c_double), _I]),
     "fc_launch_count": (_I, []),
     "fc_conv3d_device_noalloc": (_I, [_P, _P, _IP, _P, _IP, _I, _P]),
+    "fc_device_wait_status": (_I, [_P]),
+    "fc_test_set_wait_fault": (_I, [ctypes.c_longlong, _I]),
+    "fc_fault_inject": (_I, [ctypes.c_char_p]),
 }
 
 

@@ -66,14 +66,34 @@ __device__ __forceinline__ bool bar_try_wait(uint64_t* bar, uint32_t parity) {
 
 constexpr long long kWaitCycles = 1LL << 31;  // about one second at GB300 clocks
 
+// Control of the bounded waits, one copy per translation unit and device (set
+// from the host by wait_ctl_set_tu): the clock-cycle limit of one wait (0:
+// kWaitCycles), and a test switch under which the kernels arm their barriers
+// for the copies' bytes but issue no copy, so that every wait runs out with
+// nothing in flight and the kernel returns its timeout status.
+struct WaitCtl {
+  long long limit;
+  int skip_copies;
+};
+[[maybe_unused]] static __device__ WaitCtl g_wait_ctl = {0, 0};
+
+__device__ __forceinline__ bool copies_skipped() { return *(volatile int*)&g_wait_ctl.skip_copies != 0; }
+
 // wait for the phase with the given parity to complete; false on timeout
 __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
   if (bar_try_wait(bar, parity)) return true;
+  const long long lim = g_wait_ctl.limit > 0 ? g_wait_ctl.limit : kWaitCycles;
   const long long t0 = clock64();
   while (!bar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > lim) return false;
   }
   return true;
+}
+
+// host: set this translation unit's wait control on the current device
+static inline cudaError_t wait_ctl_set_tu(long long limit, int skip_copies) {
+  const WaitCtl w{limit, skip_copies ? 1 : 0};
+  return cudaMemcpyToSymbol(g_wait_ctl, &w, sizeof(w));
 }
 
 // per-thread 16-byte asynchronous copy global -> shared (cp.async, L1 bypass);

@@ -245,7 +245,8 @@ __global__ void __launch_bounds__(ZTile<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zco
     __syncthreads();
     if (threadIdx.x == 0) {
       async::bar_expect(bar, Z::STAGE_BYTES);
-      async::tensor_load_3d(stage, &tmap, (int)blockIdx.x * G::B, (int)blockIdx.y, 0, bar);
+      if (!async::copies_skipped())
+        async::tensor_load_3d(stage, &tmap, (int)blockIdx.x * G::B, (int)blockIdx.y, 0, bar);
     }
   }
   body_zconv<N, CONJ, tc::kNone, G>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, W, (int)blockIdx.x,

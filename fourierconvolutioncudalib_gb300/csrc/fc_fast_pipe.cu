@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
     const long long nr = (nrows - r0) < P::ROWS ? (nrows - r0) : P::ROWS;
     const uint32_t bytes = (uint32_t)(nr * row_bytes);
     async::bar_expect(&bar, bytes);
-    async::bulk_load(buf, in + r0 * row_bytes, bytes, &bar);
+    if (!async::copies_skipped()) async::bulk_load(buf, in + r0 * row_bytes, bytes, &bar);
   };
   if (tid == 0 && tile < ntiles) issue(tile);
   uint32_t phase = 0;
@@ -158,5 +158,7 @@ void pipe_timeouts_clear() {
   const unsigned int zero = 0;
   cudaMemcpyToSymbol(fast::g_pipe_timeouts, &zero, sizeof(zero));
 }
+
+cudaError_t pipe_wait_ctl_set(long long limit, int skip_copies) { return async::wait_ctl_set_tu(limit, skip_copies); }
 
 }  // namespace fc

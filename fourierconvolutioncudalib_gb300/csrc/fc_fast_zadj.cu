@@ -52,6 +52,7 @@ cudaError_t zadj_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
   return fast::zstage_timeouts_read_async_tu(dst, st);
 }
 void zadj_timeouts_clear() { fast::zstage_timeouts_clear_tu(); }
+cudaError_t zadj_wait_ctl_set(long long limit, int skip_copies) { return async::wait_ctl_set_tu(limit, skip_copies); }
 
 cudaError_t fast_zcorr(const float2* X, const float2* G_, float2* out, long long pitch, int ny, int ncols, int kz,
                        int hz, float scale, const FcAxis& az, cudaStream_t st) {

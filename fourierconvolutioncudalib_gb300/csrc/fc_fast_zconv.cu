@@ -91,6 +91,7 @@ cudaError_t zconv_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
   return fast::zstage_timeouts_read_async_tu(dst, st);
 }
 void zconv_timeouts_clear() { fast::zstage_timeouts_clear_tu(); }
+cudaError_t zconv_wait_ctl_set(long long limit, int skip_copies) { return async::wait_ctl_set_tu(limit, skip_copies); }
 
 void zstage_prepare() { (void)fast::tensor_map_encoder(); }
 

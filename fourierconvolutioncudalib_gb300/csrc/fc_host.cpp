@@ -15,6 +15,7 @@
 #include <chrono>
 #include <cmath>
 #include <fstream>
+#include <functional>
 #include <sstream>
 #include <cstdio>
 #include <cstdlib>
@@ -65,6 +66,50 @@ static void cuda_check(cudaError_t e, const char* what) {
     const int code = (e == cudaErrorMemoryAllocation) ? FC_ERR_NOMEM : FC_ERR_CUDA;
     FC_THROW(code, std::string(what) + ": " + cudaGetErrorString(e));
   }
+}
+
+// ------------------------------------------------------------------ allocation fault injection
+// FC_FAULT_INJECT=alloc:n, or fc_fault_inject("alloc:n"), makes the n-th
+// device or page-locked allocation of this library from then on fail as if
+// the device were out of memory (n >= 1; "off" disables it).  The failure is
+// made on the host before the CUDA call, so nothing of it reaches the GPU; it
+// exercises the error paths that a real allocation failure takes.
+static std::mutex g_fault_mu;
+static long long g_fault_alloc_at = -1;  // -1: environment not read yet; 0: off
+static long long g_fault_alloc_seen = 0;
+
+// 0 on success with *n set (0 = off), -1 for a malformed specification
+static int parse_fault_spec(const char* spec, long long* n) {
+  *n = 0;
+  if (!spec || !*spec || std::strcmp(spec, "off") == 0 || std::strcmp(spec, "0") == 0) return 0;
+  if (std::strncmp(spec, "alloc:", 6) != 0) return -1;
+  char* end = nullptr;
+  const long long v = std::strtoll(spec + 6, &end, 10);
+  if (end == spec + 6 || *end != '\0' || v < 1) return -1;
+  *n = v;
+  return 0;
+}
+
+static bool fault_alloc_now() {
+  std::lock_guard<std::mutex> lk(g_fault_mu);
+  if (g_fault_alloc_at < 0) {
+    long long n = 0;
+    g_fault_alloc_at = parse_fault_spec(std::getenv("FC_FAULT_INJECT"), &n) == 0 ? n : 0;
+  }
+  if (g_fault_alloc_at == 0) return false;
+  if (++g_fault_alloc_seen < g_fault_alloc_at) return false;
+  g_fault_alloc_at = 0;  // one failure per arming
+  return true;
+}
+
+static void dev_malloc(void** p, size_t bytes, const char* what) {
+  if (fault_alloc_now()) FC_THROW(FC_ERR_NOMEM, std::string(what) + ": injected allocation failure (FC_FAULT_INJECT)");
+  cuda_check(cudaMalloc(p, bytes), what);
+}
+
+static void host_alloc(void** p, size_t bytes, const char* what) {
+  if (fault_alloc_now()) FC_THROW(FC_ERR_NOMEM, std::string(what) + ": injected allocation failure (FC_FAULT_INJECT)");
+  cuda_check(cudaHostAlloc(p, bytes, 0), what);
 }
 
 // ------------------------------------------------------------------ radix plans
@@ -183,7 +228,7 @@ static void grow(void** p, size_t* cap, size_t need, const char* what) {
     *p = nullptr;
     *cap = 0;
   }
-  cuda_check(cudaMalloc(p, need), what);
+  dev_malloc(p, need, what);
   *cap = need;
 }
 
@@ -198,7 +243,7 @@ static const float2* twiddles_for(DevCtx& c, int n) {
     h[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
   }
   float2* d = nullptr;
-  cuda_check(cudaMalloc(&d, sizeof(float2) * (size_t)fast_twiddle_count(n)), "cudaMalloc(twiddles)");
+  dev_malloc((void**)&d, sizeof(float2) * (size_t)fast_twiddle_count(n), "cudaMalloc(twiddles)");
   cuda_check(cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice), "cudaMemcpy(twiddles)");
   cuda_check(launch_stage_twiddles(d, n, nullptr), "stage twiddles");
   cuda_check(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize(twiddles)");
@@ -565,12 +610,21 @@ static void enqueue_xy_fwd(const Geom& g, const Axes& a, const Tiles& t, const f
                       st));
 }
 
+// Set by a synchronous host entry point around its enqueue: called just before
+// the pass that writes the result, so that the entry can check the earlier
+// passes' bounded waits before the caller's buffer is touched.
+static thread_local const std::function<void()>* t_before_result_pass = nullptr;
+static void before_result_pass() {
+  if (t_before_result_pass) (*t_before_result_pass)();
+}
+
 static void enqueue_yx_inv(const Geom& g, const Axes& a, const Tiles& t, float2* S, float* d_out, cudaStream_t st,
                            const char* yname, const char* xname) {
   const long long rows = (long long)g.ny * g.nz;
   FC_PASS(yname, 16.0 * g.nxh * rows, st,
           d_cols(S, S, (long long)g.ny * g.pitch, g.pitch, g.nxh, g.nz, true, a.y, t.y_cols_log2, t.threads,
                       st));
+  before_result_pass();
   FC_PASS(xname, 4.0 * g.N() + 8.0 * g.nxh * rows, st, d_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
 }
 
@@ -671,6 +725,7 @@ static void enqueue_conv_core(const Geom& g0, const Axes& a, const float* d_imag
     FC_PASS("image_y_inv", 16.0 * w * (double)rows, st,
             d_cols(S + c0, S + c0, ps, g.pitch, w, g.nz, true, a.y, t.y_cols_log2, t.threads, st));
   }
+  before_result_pass();
   FC_PASS("image_x_c2r", 4.0 * g.N() + 8.0 * g.nxh * rows, st,
           d_x_c2r(S, g.pitch, d_out, g.nx, rows, a.x, t, st));
 }
@@ -1018,7 +1073,7 @@ static bool host_buffer_pinned(const void* p) {
 // passes): enqueue reads of their expiry counts on st, to be checked after
 // the stream's synchronisation by check_device_timeouts.
 static void enqueue_timeout_reads(DevCtx& c, cudaStream_t st) {
-  if (!c.h_timeouts) cuda_check(cudaHostAlloc((void**)&c.h_timeouts, 4 * sizeof(unsigned int), 0), "cudaHostAlloc");
+  if (!c.h_timeouts) host_alloc((void**)&c.h_timeouts, 4 * sizeof(unsigned int), "cudaHostAlloc(wait counts)");
   cuda_check(pipe_timeouts_read_async(c.h_timeouts, st), "timeout count read");
   cuda_check(zconv_timeouts_read_async(c.h_timeouts + 1, st), "timeout count read");
   cuda_check(zadj_timeouts_read_async(c.h_timeouts + 2, st), "timeout count read");
@@ -1053,24 +1108,38 @@ static void host_conv(const float* im, float* out, int nx, int ny, int nz, const
   grow(&c.ws, &c.ws_cap, wsb, "cudaMalloc(workspace)");
   grow((void**)&c.d_ker, &c.ker_cap, nker, "cudaMalloc(kernel)");
   cuda_check(cudaMemcpyAsync(c.d_ker, kernel, nker, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(kernel H2D)");
-  const int mode = host_io_mode();
-  if (allow_direct && mode != 0 && device_reads_pageable(dev) && (mode == 1 || host_buffer_pinned(im))) {
-    {
-      HostSrcScope hs(true);
-      run(im, out);
-    }
+  // every bounded device wait is checked before the result reaches `out`, so
+  // that a failed call leaves the caller's buffer as it was
+  auto check_waits = [&] {
     enqueue_timeout_reads(c, st);
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     check_device_timeouts(c);
+  };
+  const int mode = host_io_mode();
+  if (allow_direct && mode != 0 && device_reads_pageable(dev) && (mode == 1 || host_buffer_pinned(im))) {
+    // direct: the last pass writes `out` itself; the waits of the passes
+    // before it are checked first (one extra synchronisation).  The last
+    // pass's own waits (on copies from device memory) are checked after it:
+    // a pass whose first wait expires stores nothing, so `out` stays as it
+    // was unless a wait expires part-way through that pass.
+    const std::function<void()> hook = check_waits;
+    {
+      HostSrcScope hs(true);
+      struct HookScope {
+        explicit HookScope(const std::function<void()>* h) { t_before_result_pass = h; }
+        ~HookScope() { t_before_result_pass = nullptr; }
+      } hk(&hook);
+      run(im, out);
+    }
+    check_waits();
     return;
   }
   grow((void**)&c.d_img, &c.img_cap, nimg, "cudaMalloc(image)");
   cuda_check(cudaMemcpyAsync(c.d_img, im, nimg, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync(image H2D)");
   run(c.d_img, c.d_img);
+  check_waits();
   cuda_check(cudaMemcpyAsync(out, c.d_img, nimg, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync(result D2H)");
-  enqueue_timeout_reads(c, st);
   cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-  check_device_timeouts(c);
 }
 
 template <class F>
@@ -1590,7 +1659,7 @@ static void enqueue_batched(DevCtx& c, int nv, const float* const* imgs, float* 
     if (ntask) {
       std::vector<BTask> all;
       for (int p = 0; p < 5; ++p) all.insert(all.end(), e->tasks[p].begin(), e->tasks[p].end());
-      cuda_check(cudaMalloc(&e->d_tasks, sizeof(BTask) * ntask), "cudaMalloc(work-list)");
+      dev_malloc((void**)&e->d_tasks, sizeof(BTask) * ntask, "cudaMalloc(work-list)");
       cuda_check(cudaMemcpy(e->d_tasks, all.data(), sizeof(BTask) * ntask, cudaMemcpyHostToDevice),
                  "cudaMemcpy(work-list)");
     }
@@ -1703,6 +1772,42 @@ void fc_set_host_io(int mode) { g_host_io = (mode >= 0 && mode <= 2) ? mode : 2;
 void fc_set_l2_chunk_bytes(long long bytes) { g_l2_chunk_bytes = bytes < 0 ? -1 : bytes; }
 const char* fc_version(void) { return "fc-gb300 0.1.0 (sm_103a)"; }
 int fc_launch_count(void) { return t_launches; }
+
+int fc_fault_inject(const char* spec) {
+  clear_status();
+  long long n = 0;
+  if (parse_fault_spec(spec, &n) != 0) {
+    set_status(FC_ERR_ARG, "fault specification must be \"alloc:n\" (n >= 1) or \"off\"");
+    return FC_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lk(g_fault_mu);
+  g_fault_alloc_at = n;
+  g_fault_alloc_seen = 0;
+  return FC_OK;
+}
+
+int fc_device_wait_status(void* stream) {
+  clear_status();
+  return guarded([&] {
+    DevCtx& c = ctx_for(current_device());
+    std::lock_guard<std::mutex> lk(c.mu);
+    const cudaStream_t st = (cudaStream_t)stream;
+    enqueue_timeout_reads(c, st);
+    cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    check_device_timeouts(c);
+  });
+}
+
+int fc_test_set_wait_fault(long long limit_cycles, int skip_copies) {
+  clear_status();
+  return guarded([&] {
+    if (limit_cycles < 0) FC_THROW(FC_ERR_ARG, "limit_cycles must be >= 0 (0 selects the default)");
+    (void)ctx_for(current_device());
+    cuda_check(pipe_wait_ctl_set(limit_cycles, skip_copies), "wait control (x passes)");
+    cuda_check(zconv_wait_ctl_set(limit_cycles, skip_copies), "wait control (fused z pass)");
+    cuda_check(zadj_wait_ctl_set(limit_cycles, skip_copies), "wait control (adjoint z pass)");
+  });
+}
 
 int fc_plan_radices(int n, int* radices, int max_stages) {
   if (!radices || max_stages < 1) return -1;

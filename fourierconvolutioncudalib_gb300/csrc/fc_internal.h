@@ -129,6 +129,12 @@ cudaError_t zconv_timeouts_read_async(unsigned int* dst, cudaStream_t st);
 void zconv_timeouts_clear();
 cudaError_t zadj_timeouts_read_async(unsigned int* dst, cudaStream_t st);
 void zadj_timeouts_clear();
+// wait control of the bounded waits of each translation unit with bounded waits
+// (limit in clock cycles, 0 = the default of about one second; skip_copies: the
+// test switch that arms barriers without issuing their copies), current device
+cudaError_t pipe_wait_ctl_set(long long limit, int skip_copies);
+cudaError_t zconv_wait_ctl_set(long long limit, int skip_copies);
+cudaError_t zadj_wait_ctl_set(long long limit, int skip_copies);
 // resolve the tensor-map encoder of the fused z pass's stage copy (host; call
 // outside stream capture, e.g. when a device context is created)
 void zstage_prepare();

@@ -35,6 +35,14 @@
 
 typedef float imageType; /* reference src/convolution3Dfft.h:17 */
 
+/* Compile-time constants of the reference header (src/convolution3Dfft.h:18-21),
+ * kept with the same names, types and values for callers that use them.  This
+ * library's kernels do not depend on them: their launch shapes are chosen per
+ * transform length for sm_103a. */
+static const int MAX_THREADS_CUDA = 1024;
+static const int MAX_BLOCKS_CUDA = 65535;
+static const int dimsImage = 3;
+
 /* ------------------------------------------------------------------ *
  * Reference-compatible exports                                         *
  * ------------------------------------------------------------------ */
@@ -249,6 +257,32 @@ FUNCTION_PREFIX int fc_profile_read(char* names, int name_stride, float* ms, dou
 /* number of kernel launches the most recent fc_* / reference call made */
 FUNCTION_PREFIX int fc_launch_count(void);
 
+/* Failure reporting of the asynchronous entry points (no reference
+ * counterpart; the reference ends the process with exit() on any CUDA error,
+ * src/book.h:22-30).  The pipelined x passes and the fused z passes wait on
+ * asynchronous copies with a bounded wait (about one second); an expired wait
+ * ends the kernel and is counted on the device.  The synchronous entry points
+ * (convolution3DfftCUDA*, fc_* with a host buffer) check the counts before
+ * the result reaches the caller's buffer and fail with FC_ERR_TIMEOUT, leaving
+ * it unchanged.  The fc_*_device entry points return when their work is
+ * enqueued; fc_device_wait_status synchronises `stream` and returns
+ * FC_ERR_TIMEOUT if a wait on the current device has expired since the last
+ * check (then the outputs of that work are undefined), else FC_OK. */
+FUNCTION_PREFIX int fc_device_wait_status(void* stream);
+
+/* Test controls of the failure paths (no reference counterpart).
+ * fc_test_set_wait_fault sets, for the current device, the limit of the
+ * bounded waits in clock cycles (0: the default) and, with skip_copies != 0,
+ * makes the kernels arm their copy barriers without issuing the copies, so
+ * that every wait runs out with no copy in flight and each kernel returns its
+ * timeout status; (0, 0) restores normal operation.  fc_fault_inject("alloc:n")
+ * makes the n-th device or page-locked allocation of this library from then on
+ * fail with FC_ERR_NOMEM, on the host and before any CUDA call ("off"
+ * disarms; the environment variable FC_FAULT_INJECT sets it at load time).
+ * Both return FC_OK or FC_ERR_ARG. */
+FUNCTION_PREFIX int fc_test_set_wait_fault(long long limit_cycles, int skip_copies);
+FUNCTION_PREFIX int fc_fault_inject(const char* spec);
+
 /* Allocation-free variant of fc_conv3d_device (no counterpart in the
  * reference).  For callers that cannot allocate device memory when they
  * convolve -- a framework that has reserved the GPU's memory in its own pool,
@@ -257,13 +291,15 @@ FUNCTION_PREFIX int fc_launch_count(void);
  * and result as fc_conv3d_device (fp32 path, FC_FLAG_SHIFT_COMPAT and
  * FC_FLAG_DENSE_KERNEL honoured) but no workspace argument: all scratch,
  * including the twiddle tables, comes from one static device array of
- * FC_NOALLOC_SCRATCH_BYTES per device, held by every process that loads the
- * library until it exits.  A convolution needing more scratch than that is
- * rejected with FC_ERR_NOMEM and a message giving both sizes (e.g. a
- * 256x256x128 image with a 31x31x63 kernel needs about 56 MiB).  The first
- * call on a device looks up the array's device address, so make it before any
- * stream capture.  Calls share the array: calls that overlap on the GPU race
- * and must be serialised by the caller. */
+ * FC_NOALLOC_SCRATCH_BYTES per device.  Under CUDA's lazy module loading (the
+ * default since CUDA 12.2) the array is reserved when the first call on a
+ * device loads it, and then held until the process exits: make that first
+ * call at start-up, before a memory pool takes the GPU's memory and before any
+ * stream capture.  A convolution needing more scratch than that is rejected
+ * with FC_ERR_NOMEM and a message giving both sizes (e.g. a 256x256x128 image
+ * with a 31x31x63 kernel needs about 56 MiB).  Each call looks up the array's
+ * address for the current context.  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
 #define FC_NOALLOC_SCRATCH_BYTES (64ull << 20)
 FUNCTION_PREFIX int fc_conv3d_device_noalloc(const float* d_image, float* d_out, const int* imDim,
                                              const float* d_kernel, const int* kernelDim, int flags, void* stream);

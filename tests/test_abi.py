@@ -123,6 +123,24 @@ def test_argument_validation_without_gpu(fclib):
         fc.convolution3DfftCUDAInPlace(im, (4, 4, 4), np.ones((3, 3), np.float32), (3, 3, 1), 0)
 
 
+def test_fault_controls_validate_without_gpu(fclib):
+    """The failure-path test controls check their arguments on the host:
+    allocation fault specifications are "alloc:n" (n >= 1) or "off", and a
+    negative wait limit is refused before any device is touched."""
+    import fourierconvolutioncudalib_gb300 as fc
+
+    L = fc.lib()
+    try:
+        for good in (b"alloc:1", b"alloc:25", b"off", b""):
+            assert L.fc_fault_inject(good) == fc.FC_OK, good
+        for bad in (b"alloc:0", b"alloc:-2", b"alloc:", b"alloc:3x", b"free:1", b"oom"):
+            assert L.fc_fault_inject(bad) == fc.FC_ERR_ARG, bad
+            assert "alloc:n" in L.fc_last_error().decode()
+    finally:
+        assert L.fc_fault_inject(b"off") == fc.FC_OK
+    assert L.fc_test_set_wait_fault(-1, 0) == fc.FC_ERR_ARG
+
+
 def test_version_and_cuda_version(fclib):
     import fourierconvolutioncudalib_gb300 as fc
 
@@ -217,9 +235,11 @@ def test_device_wrappers_refuse_host_tensors(fclib):
 
 
 def test_header_compiles_as_c_and_links_from_cpp(fclib, tmp_path):
-    """include/convolution3Dfft.h is usable from C (C99) and from C++, and a
-    C++ program that calls the reference entry points links against the
-    library by its JNA name (built, not run: running needs a GPU)."""
+    """include/convolution3Dfft.h is usable from C (C99) and from C++, with
+    the reference header's constants (MAX_THREADS_CUDA, MAX_BLOCKS_CUDA,
+    dimsImage; src/convolution3Dfft.h:18-21), and a C++ program that calls
+    the reference entry points links against the library by its JNA name
+    (built, not run: running needs a GPU)."""
     import shutil
 
     import fourierconvolutioncudalib_gb300 as fc
@@ -231,12 +251,16 @@ def test_header_compiles_as_c_and_links_from_cpp(fclib, tmp_path):
     c_src = tmp_path / "use.c"
     c_src.write_text('#include "convolution3Dfft.h"\n'
                      'int main(void) { int d[3] = {8, 8, 8}; float im[512], k[27];\n'
-                     '  convolution3DfftCUDAInPlace(im, d, k, d, 0); return fc_last_status(); }\n')
+                     '  convolution3DfftCUDAInPlace(im, d, k, d, 0);\n'
+                     '  return fc_last_status() + (MAX_THREADS_CUDA != 1024) + (MAX_BLOCKS_CUDA != 65535)\n'
+                     '         + (dimsImage != 3); }\n')
     subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", inc, "-c", str(c_src), "-o",
                     str(tmp_path / "use.o")], check=True)
     cpp_src = tmp_path / "use.cpp"
     cpp_src.write_text('#include "convolution3Dfft.h"\n'
-                       'int main() { int d[3] = {8, 8, 8}; float* out = convolution3DfftCUDA(nullptr, d, nullptr, d, 0);\n'
+                       'static_assert(MAX_THREADS_CUDA == 1024 && MAX_BLOCKS_CUDA == 65535 && dimsImage == 3, "");\n'
+                       'int main() { int d[dimsImage] = {8, 8, 8};\n'
+                       '  float* out = convolution3DfftCUDA(nullptr, d, nullptr, d, 0);\n'
                        '  fc_free_result(out); return getNumDevicesCUDA() < 0; }\n')
     lib = fc.library_path()
     subprocess.run([gxx, "-std=c++11", "-Wall", "-Wextra", "-Werror", "-I", inc, str(cpp_src), "-L", str(lib.parent),
