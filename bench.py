@@ -14,9 +14,7 @@ Line fields (one JSON line from rank 0):
             (256 MiB write, outside the step events), mean over K steps, max
             over ranks; whole-job aggregate over N replicas.
   e2e       the same metric through convolution3DfftCUDAInPlace with host
-            buffers (pinned), H2D + compute + D2H inside the timed call.
-  roofline  the dominant pass, algorithmic bytes / its mean event duration,
-            against the measured HBM copy bandwidth.
+            buffers (pinned), H2D + compute + D2H inside the timed call;
             e2e.link holds the measured pinned copy bandwidth of the host
             link and the time the call's bytes need over it.
   roofline  the dominant pass, algorithmic bytes / its mean event duration,
@@ -675,8 +673,9 @@ def time_forms(dev, fcd, torch):
     ref2, _ = fp64_conv(im2, k2)
     i2 = torch.from_numpy(im2).to(dev)
     k2t = torch.from_numpy(k2).to(dev)
-    tc["how"] = ("radix-16 stages as 32x32 real DFT products, mma.sync m16n8k16, per-column power-of-two scaling, "
-                 "hi+lo 16-bit operands, fp32 accumulation")
+    tc["how"] = ("radix-16 stages as real 128x32x32 DFT products on tcgen05 (kind::f16, M=128 butterflies per "
+                 "128-thread group, fp32 accumulator in TMEM, operands in shared memory), per-row power-of-two "
+                 "scaling, hi+lo 16-bit operands (3 products), fp32 accumulation")
     out["tensor_core"] = tc
     # the non-power-of-two microscope stack (384x448x96, same generator and PSF): radices 16, 14, 12, 6, 2
     db = W.c2(nonpow2=True)

@@ -96,6 +96,35 @@ static inline cudaError_t wait_ctl_set_tu(long long limit, int skip_copies) {
   return cudaMemcpyToSymbol(g_wait_ctl, &w, sizeof(w));
 }
 
+// Programmatic dependent launch (sm_90 and later).  A kernel launched with
+// launch_pdl may start while the kernel before it on the stream is still
+// running: it signals at once that its own successor may launch
+// (pdl_launch_dependents), sets up its shared memory, and then waits for its
+// predecessor to complete and its memory to be visible (pdl_wait) before it
+// reads anything that kernel wrote.  Both are no-ops for a kernel launched
+// without the attribute.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// FC_PDL=0 launches the persistent pass kernels without programmatic dependent launch
+bool pdl_enabled();
+
+template <class K, class... Args>
+static inline cudaError_t launch_pdl(K kern, unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                                     Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // per-thread 16-byte asynchronous copy global -> shared (cp.async, L1 bypass);
 // both addresses 16-byte aligned.  Completion: commit(), then wait_all() in the
 // issuing thread, then a CTA barrier before other threads read the data.

@@ -11,10 +11,18 @@
 namespace fc {
 namespace fast {
 
+// the task holding global tile g: the last task whose tile0 <= g (tasks sorted
+// by tile0, tasks[0].tile0 == 0), by binary search
 __device__ __forceinline__ int find_task(const BTask* __restrict__ tasks, int ntasks, long long g) {
-  int i = 0;
-  while (i + 1 < ntasks && tasks[i + 1].tile0 <= g) ++i;
-  return i;
+  int lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tasks[mid].tile0 <= g)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
 }
 
 template <int N>

@@ -20,17 +20,16 @@
 //     between a forward and an inverse transform happens in registers.
 #pragma once
 #include "fc_fft.cuh"
-#include "fc_tc.cuh"
+#include "fc_tc5.cuh"
 
 namespace fc {
 namespace fast {
 
 constexpr int kVals = 16;  // values per thread
 
-// tensor-core mode context: per-warp scratch and the CTA's A-fragment table
+// tensor-core mode context: the CTA's tcgen05 state (operands, mbarrier, TMEM)
 struct TcCtx {
-  uint32_t* ws;
-  const uint32_t* tab;
+  const tc::Tc5* t5;
 };
 
 __host__ __device__ constexpr int pick_radix(int rem) {
@@ -163,8 +162,10 @@ __host__ __device__ constexpr bool lin_read(int NB) {
 }
 
 // stage I of the forward chain (REV = false) or of the reversed chain (REV = true);
-// INV selects the conjugate twiddles and DFT roots
-template <int N, int I, int R, int NS, bool INV, int TCM, bool REV = INV>
+// INV selects the conjugate twiddles and DFT roots.  TWS: W is a copy of the
+// chain's stage tables alone (its first entry is stage 1's), typically in
+// shared memory, instead of the whole global table of the axis.
+template <int N, int I, int R, int NS, bool INV, int TCM, bool REV = INV, bool TWS = false>
 __device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const float2* __restrict__ W,
                                       const TcCtx& tcx) {
   constexpr int U = kVals / R;
@@ -176,12 +177,18 @@ __device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const flo
   for (int b = 0; b < U; ++b) {
     if (NS > 1) {
       const int k = (t + b * A) % NS;
-      const float2* tw = W + Plan<N>::tab_off(REV, I) + k;
+      if constexpr (TWS) {
+        const float2* tw = W + (Plan<N>::tab_off(REV, I) - Plan<N>::tab_off(REV, 1)) + k;
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[b * R + r] = c_tw<INV>(v[b * R + r], __ldg(tw + (r - 1) * NS));
+        for (int r = 1; r < R; ++r) v[b * R + r] = c_tw<INV>(v[b * R + r], tw[(r - 1) * NS]);
+      } else {
+        const float2* tw = W + Plan<N>::tab_off(REV, I) + k;
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[b * R + r] = c_tw<INV>(v[b * R + r], __ldg(tw + (r - 1) * NS));
+      }
     }
     if constexpr (TCM != tc::kNone && R == 16)
-      tc::dft16<INV, TCM>(&v[b * R], tcx.ws, tcx.tab);
+      tc::dft16<INV, TCM>(&v[b * R], *tcx.t5);
     else
       Dft<R, INV>::run(&v[b * R]);
   }
@@ -228,17 +235,17 @@ __device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const 
 }
 
 // stages I .. S-1 of the forward chain (INV = false) or of the reversed chain (INV = true)
-template <int N, int I, int NS, bool INV, int TCM, bool REV = INV>
+template <int N, int I, int NS, bool INV, int TCM, bool REV = INV, bool TWS = false>
 struct Chain {
   template <class L>
   static __device__ __forceinline__ void run(float2 (&v)[kVals], const L& sm, const int t,
                                              const float2* __restrict__ W, const TcCtx& tcx) {
     constexpr int R = Plan<N>::radix(I, REV);
-    stage<N, I, R, NS, INV, TCM, REV>(v, t, W, tcx);
+    stage<N, I, R, NS, INV, TCM, REV, TWS>(v, t, W, tcx);
     if constexpr (I + 1 < Plan<N>::S) {
       constexpr int R2 = Plan<N>::radix(I + 1, REV);
       exchange<N, R, NS, R2>(v, sm, t);
-      Chain<N, I + 1, NS * R, INV, TCM, REV>::run(v, sm, t, W, tcx);
+      Chain<N, I + 1, NS * R, INV, TCM, REV, TWS>::run(v, sm, t, W, tcx);
     }
   }
 };
@@ -248,10 +255,20 @@ struct Chain {
 // REV: radix order (false: the forward chain, true: the reversed chain).  A
 // transform that consumes another's outputs in registers runs the other's
 // order reversed; a standalone pass may run either.
-template <int N, bool INV, int TCM = tc::kNone, bool REV = INV, class L>
+template <int N, bool INV, int TCM = tc::kNone, bool REV = INV, bool TWS = false, class L>
 __device__ __forceinline__ void fft(float2 (&v)[kVals], const L& sm, const int t, const float2* __restrict__ W,
-                                    const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
-  Chain<N, 0, 1, INV, TCM, REV>::run(v, sm, t, W, tcx);
+                                    const TcCtx& tcx = TcCtx{nullptr}) {
+  Chain<N, 0, 1, INV, TCM, REV, TWS>::run(v, sm, t, W, tcx);
+}
+
+// Stage tables of one chain: Plan<N>::tab_size(REV) entries starting at the
+// axis table's tab_off(REV, 1); copy_stage_tables copies them (all threads of
+// the CTA take part; a barrier must follow before use) for fft<..., TWS=true>.
+template <int N, bool REV>
+__device__ __forceinline__ void copy_stage_tables(float2* dst, const float2* __restrict__ W, int tid, int nthreads) {
+  constexpr int n = Plan<N>::tab_size(REV);
+  const float2* src = W + Plan<N>::tab_off(REV, 1);
+  for (int i = tid; i < n; i += nthreads) dst[i] = __ldg(src + i);
 }
 
 // radix of the first / last stage of the forward (INV=false) or inverse chain

@@ -14,6 +14,8 @@
 #endif
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "fc_async.cuh"
 #include "fc_fast.cuh"
 #include "fc_fast_sizes.h"
@@ -48,7 +50,7 @@ using ColGeomWide = ColGeomB<N, 32, 512, 8192>;
 template <int N, bool INV, class Src, int TCM = tc::kNone, class G = ColGeom<N>, bool REV = INV>
 __device__ __forceinline__ void body_cols(const Src& src, float2* dst, long long ps, long long es, int ncols,
                                           const float2* __restrict__ W, int bx, int plane, int tid, float2* sm,
-                                          const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+                                          const TcCtx& tcx = TcCtx{nullptr}) {
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, REV>(), RF = last_radix<N, REV>();
   const int c = tid % B;
@@ -151,7 +153,7 @@ template <int N, bool CONJ, int TCM = tc::kNone, class G = ColGeom<N>>
 __device__ __forceinline__ void body_zconv(float2* __restrict__ S, const float2* __restrict__ KXY, long long pitch,
                                            int ny, int ncols, int kplanes, int hz, float scale,
                                            const float2* __restrict__ W, int bx, int ky, int tid, float2* sm,
-                                           float2* stash, int nstash, const TcCtx& tcx = TcCtx{nullptr, nullptr},
+                                           float2* stash, int nstash, const TcCtx& tcx = TcCtx{nullptr},
                                            float2* stage = nullptr, uint64_t* bar = nullptr) {
   constexpr int B = G::B;
   constexpr int R0 = first_radix<N, kZRev>(), RF = last_radix<N, !kZRev>();
@@ -251,7 +253,187 @@ __global__ void __launch_bounds__(ZTile<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zco
   }
   body_zconv<N, CONJ, tc::kNone, G>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, W, (int)blockIdx.x,
                                     (int)blockIdx.y, (int)threadIdx.x, zsm, stash, G::THREADS,
-                                    TcCtx{nullptr, nullptr}, stage, bar);
+                                    TcCtx{nullptr}, stage, bar);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent fused z pass.  Each CTA walks the tiles (B columns x N planes of
+// one row ky) with a stride of the grid size; both operands of a tile arrive
+// in shared memory by tensor-map copies (TMA) issued one tile ahead:
+//   * the image tile (N rows of B columns) into ISTAGE, in NBOX boxes of
+//     ZBOX rows; the next tile's copy is issued as soon as every thread has
+//     read the current one into registers, so it lands behind the current
+//     tile's three transforms;
+//   * the kernel column tile (the kplanes planes of KXY that hold taps) into
+//     KSTAGE, in boxes of kbox rows (host-chosen, <= 256); once transformed,
+//     the kernel spectrum is parked in the same buffer (per-thread private
+//     slots), and the next tile's kernel copy is issued after the product has
+//     read it, so it lands behind the inverse transform and the stores.
+// The stage tables of both radix chains sit in shared memory, copied once per
+// CTA.  Every copy's destination is 128-byte aligned and every box lies
+// inside its buffer: lengths whose image boxes would start off a 128-byte
+// boundary (e.g. z = 500 on 4-column tiles, whose second 250-row box would
+// start 8000 bytes in) keep the one-tile-per-CTA kernel.  Waits are bounded:
+// a wait that runs out is counted, the CTA waits (bounded) for any copy it
+// still has in flight, and returns.
+template <int N>
+struct ZPipe {
+  using G = ZTile<N>;
+  static constexpr int B = G::B;
+  static constexpr int THREADS = G::THREADS;
+  static constexpr int XCH_BYTES = ((G::SMEM * (int)sizeof(float2) + 127) / 128) * 128;
+  static constexpr int ZBOX = zbox_rows(N);
+  static constexpr int NBOX = N / ZBOX;
+  static constexpr int IBYTES = N * B * (int)sizeof(float2);
+  static constexpr int ISTAGE_OFF = XCH_BYTES;
+  // kernel planes: at most N rows in boxes of kbox rows, each box's bytes a
+  // multiple of 128 (kbox a multiple of 16/B); capacity N + 16 rows covers the
+  // rounding; the parked kernel spectrum needs THREADS*16 slots
+  static constexpr int KROW_ALIGN = B >= 16 ? 1 : 16 / B;
+  static constexpr int KCAP = (N + 16) * B > THREADS * kVals ? (N + 16) * B : THREADS * kVals;  // float2
+  static constexpr int KSTAGE_OFF = ISTAGE_OFF + ((IBYTES + 127) / 128) * 128;
+  // stage tables of both chains (forward transforms: REV = kZRev; inverse: !kZRev)
+  static constexpr int TWF_N = Plan<N>::tab_size(kZRev), TWI_N = Plan<N>::tab_size(!kZRev);
+  static constexpr int TWF_OFF = KSTAGE_OFF + ((KCAP * (int)sizeof(float2) + 127) / 128) * 128;
+  static constexpr int TWI_OFF = TWF_OFF + ((TWF_N * (int)sizeof(float2) + 127) / 128) * 128;
+  static constexpr int BAR_OFF = TWI_OFF + ((TWI_N * (int)sizeof(float2) + 127) / 128) * 128;
+  static constexpr int SMEM_BYTES = BAR_OFF + 128;
+  static_assert(ZBOX <= 256 && ZBOX * NBOX == N, "image boxes must tile the column");
+  static_assert((B * (int)sizeof(float2)) % 16 == 0, "box rows must be multiples of 16 bytes");
+  static_assert(ISTAGE_OFF % 128 == 0 && KSTAGE_OFF % 128 == 0 && BAR_OFF % 128 == 0, "stage alignment");
+  static constexpr bool OK = (ZBOX * B * (int)sizeof(float2)) % 128 == 0 && SMEM_BYTES <= 227 * 1024;
+  static constexpr int MIN_BLOCKS = ZGeom<N>::MIN_BLOCKS;
+};
+
+template <int N, bool CONJ>
+__global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
+    k_zconv_pipe(float2* __restrict__ S, long long pitch, int ny, int ncols, int kplanes, int hz, float scale,
+                 const float2* __restrict__ W, const __grid_constant__ CUtensorMap imap,
+                 const __grid_constant__ CUtensorMap kmap, int kbox, int nkbox) {
+  using P = ZPipe<N>;
+  constexpr int B = P::B;
+  constexpr int R0 = first_radix<N, kZRev>(), RF = last_radix<N, !kZRev>();
+  extern __shared__ __align__(128) unsigned char zpsm[];
+  float2* xch = reinterpret_cast<float2*>(zpsm);
+  float2* ist = reinterpret_cast<float2*>(zpsm + P::ISTAGE_OFF);
+  float2* kst = reinterpret_cast<float2*>(zpsm + P::KSTAGE_OFF);
+  float2* twf = reinterpret_cast<float2*>(zpsm + P::TWF_OFF);
+  float2* twi = reinterpret_cast<float2*>(zpsm + P::TWI_OFF);
+  uint64_t* ibar = reinterpret_cast<uint64_t*>(zpsm + P::BAR_OFF);
+  uint64_t* kbar = ibar + 1;
+  const int tid = (int)threadIdx.x;
+  const int c = tid % B;
+  const int t = tid / B;
+  const int ntx = (ncols + B - 1) / B;
+  const long long ntiles = (long long)ntx * ny;
+  const long long zs = (long long)ny * pitch;
+  const unsigned kbytes = (unsigned)(nkbox * kbox * B * (int)sizeof(float2));
+  const bool skip = async::copies_skipped();
+  async::pdl_launch_dependents();
+  auto issue_image = [&](long long ti) {
+    const int bx = (int)(ti % ntx), ky = (int)(ti / ntx);
+    async::bar_expect(ibar, (unsigned)P::IBYTES);
+    if (!skip)
+#pragma unroll
+      for (int b = 0; b < P::NBOX; ++b)
+        async::tensor_load_3d(ist + b * P::ZBOX * B, &imap, bx * B, ky, b * P::ZBOX, ibar);
+  };
+  auto issue_kernel = [&](long long ti) {
+    const int bx = (int)(ti % ntx), ky = (int)(ti / ntx);
+    async::bar_expect(kbar, kbytes);
+    if (!skip)
+      for (int b = 0; b < nkbox; ++b) async::tensor_load_3d(kst + b * kbox * B, &kmap, bx * B, ky, b * kbox, kbar);
+  };
+  // the twiddle tables are not written by any pass
+  copy_stage_tables<N, kZRev>(twf, W, tid, P::THREADS);
+  copy_stage_tables<N, !kZRev>(twi, W, tid, P::THREADS);
+  if (tid == 0) {
+    async::bar_init(ibar, 1);
+    async::bar_init(kbar, 1);
+    async::bar_init_fence();
+  }
+  __syncthreads();
+  async::pdl_wait();  // the previous pass's output is complete and visible
+  long long ti = blockIdx.x;
+  if (tid == 0 && ti < ntiles) {
+    issue_kernel(ti);
+    issue_image(ti);
+  }
+  bool kpend = ti < ntiles, ipend = ti < ntiles;  // copies in flight (uniform)
+  bool expired = false;
+  uint32_t ph = 0;  // parity of the barriers' current phase (one phase per tile)
+  const ColLay<B> lay{xch, c};
+  for (; ti < ntiles; ti += gridDim.x, ph ^= 1u) {
+    const int ky = (int)(ti / ntx);
+    const int col = (int)(ti % ntx) * B + c;
+    const bool ok = col < ncols && t < P::G::T;
+    const long long next = ti + gridDim.x;
+    float2 v[kVals];
+    // ---- kernel column: load from KSTAGE, forward transform, park in KSTAGE
+    if (!__syncthreads_and(async::bar_wait(kbar, ph))) {
+      expired = true;
+      break;
+    }
+    kpend = false;
+#pragma unroll
+    for (int q = 0; q < kVals; ++q) {
+      const int z = stage_pos<N, R0>(t, q);
+      int p = z + hz;
+      if (p >= N) p -= N;
+      v[q] = (ok && z >= 0 && p < kplanes) ? kst[p * B + c] : make_float2(0.f, 0.f);
+    }
+    if constexpr (Plan<N>::S == 1) __syncthreads();  // no exchange barrier inside the transform
+    fft<N, false, tc::kNone, kZRev, true>(v, lay, t, twf);
+#pragma unroll
+    for (int q = 0; q < kVals; ++q) kst[q * P::THREADS + tid] = v[q];
+    // ---- image tile: load from ISTAGE, then the next tile's image copy
+    if (!__syncthreads_and(async::bar_wait(ibar, ph))) {
+      expired = true;
+      break;
+    }
+    ipend = false;
+#pragma unroll
+    for (int q = 0; q < kVals; ++q) {
+      const int z = stage_pos<N, R0>(t, q);
+      v[q] = (ok && z >= 0) ? ist[z * B + c] : make_float2(0.f, 0.f);
+    }
+    async::proxy_fence();
+    __syncthreads();  // every thread has read ISTAGE
+    if (next < ntiles) {
+      if (tid == 0) issue_image(next);
+      ipend = true;
+    }
+    fft<N, false, tc::kNone, kZRev, true>(v, lay, t, twf);
+#pragma unroll
+    for (int q = 0; q < kVals; ++q) {
+      float2 a = kst[q * P::THREADS + tid];  // kernel spectrum (d_Src of modulateAndNormalize_kernel)
+      const float2 b = v[q];                  // image spectrum  (d_Dst)
+      if (CONJ) a.y = -a.y;
+      v[q] = make_float2(scale * (a.x * b.x - a.y * b.y), scale * (a.y * b.x + a.x * b.y));
+    }
+    async::proxy_fence();
+    __syncthreads();  // every thread has read its parked kernel spectrum
+    if (next < ntiles) {
+      if (tid == 0) issue_kernel(next);
+      kpend = true;
+    }
+    fft<N, true, tc::kNone, !kZRev, true>(v, lay, t, twi);
+    if (ok) {
+      float2* base = S + (long long)ky * pitch + col;
+#pragma unroll
+      for (int q = 0; q < kVals; ++q) {
+        const int z = stage_pos<N, RF>(t, q);
+        if (z >= 0) base[(long long)z * zs] = v[q];
+      }
+    }
+  }
+  if (expired) {
+    // a wait ran out: count it, then let the copies still in flight (both of
+    // the current phase) land, with the same bounded wait, before returning
+    if (tid == 0) atomicAdd(&g_zstage_timeouts, 1u);
+    if (kpend) (void)async::bar_wait(kbar, ph);
+    if (ipend) (void)async::bar_wait(ibar, ph);
+  }
 }
 
 // Host: encode the tensor map of k_zconv's image stage for a spectrum of ncols
@@ -259,6 +441,51 @@ __global__ void __launch_bounds__(ZTile<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zco
 // driver entry point is missing or the layout breaks a tensor-map rule.
 bool zstage_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int n, int box_cols,
                        int box_rows);
+// FC_ZPIPE=0 selects the one-tile-per-CTA fused z pass instead of the persistent one
+bool zpipe_enabled();
+
+// Host: launch the persistent fused z pass when its geometry applies (sets
+// *used); otherwise enqueue nothing and leave *used false.  The kernel planes
+// come in boxes of kbox <= 256 rows, kbox a multiple of KROW_ALIGN (so that
+// every box starts 128-byte aligned), within KSTAGE's capacity.
+template <int N, bool CONJ>
+static cudaError_t zconv_pipe_launch(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes,
+                                     int hz, float scale, const float2* W, cudaStream_t st, bool* used) {
+  using P = ZPipe<N>;
+  *used = false;
+  if constexpr (!P::OK) {
+    return cudaSuccess;
+  } else {
+    if (!zpipe_enabled() || kplanes < 1 || kplanes > N || ny < 1 || ncols < 1) return cudaSuccess;
+    const int nkb = (kplanes + 255) / 256;
+    int kbox = (kplanes + nkb - 1) / nkb;
+    kbox = (kbox + P::KROW_ALIGN - 1) / P::KROW_ALIGN * P::KROW_ALIGN;
+    if (kbox > 256 || (long long)nkb * kbox * P::B > P::KCAP) return cudaSuccess;
+    CUtensorMap imap, kmap;
+    if (!zstage_tensor_map(&imap, S, pitch, ny, ncols, N, P::B, P::ZBOX) ||
+        !zstage_tensor_map(&kmap, KXY, pitch, ny, ncols, kplanes, P::B, kbox))
+      return cudaSuccess;
+    auto kern = k_zconv_pipe<N, CONJ>;
+    static int s_occ = 0;  // resident CTAs per SM of this instantiation (a benign race: same value)
+    int occ = s_occ;
+    if (occ == 0) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, P::THREADS, P::SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      if (occ < 1) return cudaSuccess;
+      s_occ = occ;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long ntiles = (long long)((ncols + P::B - 1) / P::B) * ny;
+    const long long grid = std::min<long long>(ntiles, (long long)occ * sms);
+    *used = true;
+    return async::launch_pdl(kern, (unsigned)grid, P::THREADS, P::SMEM_BYTES, st, S, pitch, ny, ncols, kplanes, hz,
+                             scale, W, imap, kmap, kbox, nkb);
+  }
+}
 // Host: enqueue a read of this translation unit's count of expired stage
 // waits into dst (page-locked host memory) on st; clear the count
 static inline cudaError_t zstage_timeouts_read_async_tu(unsigned int* dst, cudaStream_t st) {

@@ -59,16 +59,16 @@ __device__ __forceinline__ void load_r2c(float2 (&v)[kVals], const Src& src, con
 }
 
 // transform of the loaded values, separation of the two half spectra, stores
-template <int N, int TCM = tc::kNone, bool REV = false>
+template <int N, int TCM = tc::kNone, bool REV = false, bool TWS = false>
 __device__ __forceinline__ void finish_r2c(float2 (&v)[kVals], const RowSlot<N>& s, float2* __restrict__ out,
                                            long long out_pitch, const float2* __restrict__ W, float2* sm,
-                                           const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+                                           const TcCtx& tcx = TcCtx{nullptr}) {
   using G = RowGeom<N>;
   constexpr int RF = last_radix<N, REV>();
   constexpr int NBF = N / RF, UF = kVals / RF, AF = Plan<N>::A(RF);
   float2* lbase = sm + s.line * G::LS;
   const RowLay lay{lbase};
-  fft<N, false, TCM, REV>(v, lay, s.t, W, tcx);
+  fft<N, false, TCM, REV, TWS>(v, lay, s.t, W, tcx);
   // natural-order outputs x = j + m*NBF of the last stage into the line
 #pragma unroll
   for (int b = 0; b < UF; ++b) {
@@ -98,7 +98,7 @@ __device__ __forceinline__ void finish_r2c(float2 (&v)[kVals], const RowSlot<N>&
 template <int N, class Src, int TCM = tc::kNone>
 __device__ __forceinline__ void body_r2c(const Src& src, float2* __restrict__ out, long long out_pitch,
                                          long long nrows, const float2* __restrict__ W, long long tile, int tid,
-                                         float2* sm, const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+                                         float2* sm, const TcCtx& tcx = TcCtx{nullptr}) {
   const RowSlot<N> s(tile, tid, nrows);
   float2 v[kVals];
   load_r2c<N>(v, src, s);
@@ -135,13 +135,13 @@ __device__ __forceinline__ void load_c2r(float2 (&v)[kVals], const In& in, const
   }
 }
 
-template <int N, int TCM = tc::kNone, bool REV = true>
+template <int N, int TCM = tc::kNone, bool REV = true, bool TWS = false>
 __device__ __forceinline__ void finish_c2r(float2 (&v)[kVals], const RowSlot<N>& s, float* __restrict__ out,
                                            long long out_pitch, const float2* __restrict__ W, float2* sm,
-                                           const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+                                           const TcCtx& tcx = TcCtx{nullptr}) {
   using G = RowGeom<N>;
   constexpr int RF = last_radix<N, REV>();
-  fft<N, true, TCM, REV>(v, RowLay{sm + s.line * G::LS}, s.t, W, tcx);
+  fft<N, true, TCM, REV, TWS>(v, RowLay{sm + s.line * G::LS}, s.t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int x = stage_pos<N, RF>(s.t, q);
@@ -163,7 +163,7 @@ template <int N, int TCM = tc::kNone, bool REV = true>
 __device__ __forceinline__ void body_c2r(const float2* __restrict__ in, long long in_pitch, float* __restrict__ out,
                                          long long out_pitch, long long nrows, const float2* __restrict__ W,
                                          long long tile, int tid, float2* sm,
-                                         const TcCtx& tcx = TcCtx{nullptr, nullptr}) {
+                                         const TcCtx& tcx = TcCtx{nullptr}) {
   const RowSlot<N> s(tile, tid, nrows);
   float2 v[kVals];
   load_c2r<N, HalfRows, REV>(v, HalfRows{in, in_pitch}, s);

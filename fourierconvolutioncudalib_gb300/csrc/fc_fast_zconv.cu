@@ -52,6 +52,14 @@ bool zstage_use_tma() {
   return on;
 }
 
+bool zpipe_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("FC_ZPIPE");
+    return !e || std::atoi(e) != 0;
+  }();
+  return on;
+}
+
 // opt in to more than 48 KiB of dynamic shared memory where a kernel needs it
 template <class K>
 static cudaError_t set_dyn_smem(K kernel, int bytes) {
@@ -66,6 +74,10 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
   switch (az.n) {
 #define FC_CASE(n_)                                                                                             \
   case n_: {                                                                                                    \
+    bool used = false;                                                                                          \
+    const cudaError_t ep = zconv_pipe_launch<n_, CONJ>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az.W, st,   \
+                                                        &used);                                                 \
+    if (ep != cudaSuccess || used) return ep;                                                                   \
     using G = ZTile<n_>;                                                                                        \
     constexpr int sm = ZGeom<n_>::SMEM_BYTES;                                                                   \
     dim3 grid((ncols + G::B - 1) / G::B, ny);                                                                   \

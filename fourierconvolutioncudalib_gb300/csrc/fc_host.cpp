@@ -1073,16 +1073,20 @@ static bool host_buffer_pinned(const void* p) {
 // passes): enqueue reads of their expiry counts on st, to be checked after
 // the stream's synchronisation by check_device_timeouts.
 static void enqueue_timeout_reads(DevCtx& c, cudaStream_t st) {
-  if (!c.h_timeouts) host_alloc((void**)&c.h_timeouts, 4 * sizeof(unsigned int), "cudaHostAlloc(wait counts)");
+  if (!c.h_timeouts) host_alloc((void**)&c.h_timeouts, 8 * sizeof(unsigned int), "cudaHostAlloc(wait counts)");
   cuda_check(pipe_timeouts_read_async(c.h_timeouts, st), "timeout count read");
   cuda_check(zconv_timeouts_read_async(c.h_timeouts + 1, st), "timeout count read");
   cuda_check(zadj_timeouts_read_async(c.h_timeouts + 2, st), "timeout count read");
+  cuda_check(tc_timeouts_read_async_fp16(c.h_timeouts + 3, st), "timeout count read");
+  cuda_check(tc_timeouts_read_async_bf16(c.h_timeouts + 4, st), "timeout count read");
 }
 static void check_device_timeouts(DevCtx& c) {
-  if (!(c.h_timeouts[0] | c.h_timeouts[1] | c.h_timeouts[2])) return;
+  if (!(c.h_timeouts[0] | c.h_timeouts[1] | c.h_timeouts[2] | c.h_timeouts[3] | c.h_timeouts[4])) return;
   pipe_timeouts_clear();
   zconv_timeouts_clear();
   zadj_timeouts_clear();
+  tc_timeouts_clear_fp16();
+  tc_timeouts_clear_bf16();
   FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in an asynchronous copy");
 }
 

@@ -157,10 +157,11 @@ cudaError_t fast_zsub(float2* S, long long pitch, int ny, int ncols, const SubMa
                       cudaStream_t st);
 
 // Tensor-core precision mode (fc_tc.cu, compiled for fp16 and for bf16):
-// register-resident kernels whose radix-16 stages run on the tensor cores,
-// lengths 128, 256, 512, 1024.  tc_cols mode: 0 forward, 1 inverse, 2 kernel
-// forward from the compact x-spectrum rows.  tc_x_r2c: taps != NULL selects
-// the kernel-tap source (kx, hx), else the dense rows `in`.
+// register-resident kernels whose radix-16 stages run on the tcgen05 tensor
+// cores, lengths 128, 256, 512, 1024.  tc_cols mode: 0 forward, 1 inverse,
+// 2 kernel forward from the compact x-spectrum rows.  tc_x_r2c: taps != NULL
+// selects the kernel-tap source (kx, hx), else the dense rows `in`.
+// tc_timeouts_*: the count of expired waits on the MMA barrier.
 #define FC_TC_DECL(sfx)                                                                                           \
   cudaError_t tc_x_r2c##sfx(const float* in, long long in_pitch, const float* taps, int kx, int hx, float2* out,   \
                             long long out_pitch, long long nrows, const FcAxis& ax, cudaStream_t st);               \
@@ -169,7 +170,9 @@ cudaError_t fast_zsub(float2* S, long long pitch, int ny, int ncols, const SubMa
   cudaError_t tc_cols##sfx(int mode, const float2* src, long long src_pitch, int krows, int hy, float2* dst,        \
                            long long ps, long long es, int ncols, int nplanes, const FcAxis& ax, cudaStream_t st);  \
   cudaError_t tc_zconv##sfx(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,  \
-                            float scale, const FcAxis& az, cudaStream_t st);
+                            float scale, const FcAxis& az, cudaStream_t st);                                         \
+  cudaError_t tc_timeouts_read_async##sfx(unsigned int* dst, cudaStream_t st);                                       \
+  void tc_timeouts_clear##sfx();
 FC_TC_DECL(_fp16)
 FC_TC_DECL(_bf16)
 #undef FC_TC_DECL

@@ -1,11 +1,13 @@
 // Tensor-core precision mode: the register-resident pass kernels with their
-// radix-16 stages on the tensor cores (fc_tc.cuh), for the power-of-two
-// lengths FC_TC_SIZES.  This file is compiled twice, with FC_TC_MODE=1 (fp16
-// hi+lo operands) and FC_TC_MODE=2 (bf16 hi+lo operands).
+// radix-16 stages on the fifth-generation tensor cores (tcgen05, fc_tc5.cuh),
+// for the power-of-two lengths FC_TC_SIZES.  This file is compiled twice,
+// with FC_TC_MODE=1 (fp16 hi+lo operands) and FC_TC_MODE=2 (bf16 hi+lo
+// operands).
 //
 // Dynamic shared memory of every kernel: [exchange tile | stash (z pass) |
-// A-fragment table (tc::kTableWords) | per-warp scratch (tc::kWarpWords each)];
-// the table is built by the CTA at start.
+// tcgen05 area (tc::tc5_bytes, 128-byte aligned)].  Every kernel sets the
+// mode up at start (DFT operands, mbarrier, TMEM allocation) and frees its
+// TMEM at the end; no kernel of this file returns early.
 #include "fc_fast_cols.cuh"
 #include "fc_fast_rows.cuh"
 
@@ -19,41 +21,43 @@ namespace fast {
 
 constexpr int TCM = FC_TC_MODE;
 
-__device__ __forceinline__ TcCtx tc_setup(float2* after, int tid, int nthreads) {
-  uint32_t* tab = reinterpret_cast<uint32_t*>(after);
-  tc::build_table<TCM>(tab, tid, nthreads);
-  __syncthreads();
-  return TcCtx{tab + tc::kTableWords + (tid >> 5) * tc::kWarpWords, tab};
-}
+// byte offset of the tcgen05 area after `floats2` float2 of the kernel's own buffers
+__host__ __device__ constexpr size_t tc_area_off(size_t floats2) { return (floats2 * sizeof(float2) + 127) / 128 * 128; }
 
-static size_t tc_bytes(int nthreads) {
-  return sizeof(uint32_t) * (size_t)(tc::kTableWords + ((nthreads + 31) / 32) * tc::kWarpWords);
+static size_t tc_smem(size_t floats2, int nthreads) { return tc_area_off(floats2) + (size_t)tc::tc5_bytes(nthreads); }
+
+__device__ __forceinline__ tc::Tc5 tc_setup(float2* dsm, size_t floats2, int tid, int nthreads) {
+  return tc::tc5_setup<TCM>(reinterpret_cast<unsigned char*>(dsm) + tc_area_off(floats2), tid, nthreads);
 }
 
 template <int N, class Src>
 __global__ void __launch_bounds__(RowGeom<N>::THREADS) k_r2c_tc(Src src, float2* __restrict__ out, long long out_pitch,
                                                                 long long nrows, const float2* __restrict__ W) {
-  extern __shared__ float2 dsm[];
-  const TcCtx tcx = tc_setup(dsm + RowGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
-  body_r2c<N, Src, TCM>(src, out, out_pitch, nrows, W, (long long)blockIdx.x, (int)threadIdx.x, dsm, tcx);
+  extern __shared__ __align__(128) float2 dsm[];
+  const tc::Tc5 t5 = tc_setup(dsm, RowGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
+  body_r2c<N, Src, TCM>(src, out, out_pitch, nrows, W, (long long)blockIdx.x, (int)threadIdx.x, dsm, TcCtx{&t5});
+  tc::tc5_teardown(t5, (int)threadIdx.x, (int)blockDim.x);
 }
 
 template <int N>
 __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_c2r_tc(const float2* __restrict__ in, long long in_pitch,
                                                                 float* __restrict__ out, long long out_pitch,
                                                                 long long nrows, const float2* __restrict__ W) {
-  extern __shared__ float2 dsm[];
-  const TcCtx tcx = tc_setup(dsm + RowGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
-  body_c2r<N, TCM, false>(in, in_pitch, out, out_pitch, nrows, W, (long long)blockIdx.x, (int)threadIdx.x, dsm, tcx);
+  extern __shared__ __align__(128) float2 dsm[];
+  const tc::Tc5 t5 = tc_setup(dsm, RowGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
+  body_c2r<N, TCM, false>(in, in_pitch, out, out_pitch, nrows, W, (long long)blockIdx.x, (int)threadIdx.x, dsm,
+                          TcCtx{&t5});
+  tc::tc5_teardown(t5, (int)threadIdx.x, (int)blockDim.x);
 }
 
 template <int N, bool INV, class Src>
 __global__ void __launch_bounds__(ColGeom<N>::THREADS, 3) k_cols_tc(Src src, float2* dst, long long ps, long long es,
                                                                  int ncols, const float2* __restrict__ W) {
-  extern __shared__ float2 dsm[];
-  const TcCtx tcx = tc_setup(dsm + ColGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
+  extern __shared__ __align__(128) float2 dsm[];
+  const tc::Tc5 t5 = tc_setup(dsm, ColGeom<N>::SMEM, (int)threadIdx.x, (int)blockDim.x);
   body_cols<N, INV, Src, TCM, ColGeom<N>, false>(src, dst, ps, es, ncols, W, (int)blockIdx.x, (int)blockIdx.y,
-                                                 (int)threadIdx.x, dsm, tcx);
+                                                 (int)threadIdx.x, dsm, TcCtx{&t5});
+  tc::tc5_teardown(t5, (int)threadIdx.x, (int)blockDim.x);
 }
 
 template <int N>
@@ -61,12 +65,13 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_zconv_tc(float2* __rest
                                                                   const float2* __restrict__ KXY, long long pitch,
                                                                   int ny, int ncols, int kplanes, int hz, float scale,
                                                                   const float2* __restrict__ W) {
-  extern __shared__ float2 dsm[];
+  extern __shared__ __align__(128) float2 dsm[];
   constexpr int T = ColGeom<N>::THREADS;
   float2* stash = dsm + ColGeom<N>::SMEM;
-  const TcCtx tcx = tc_setup(stash + T * kVals, (int)threadIdx.x, (int)blockDim.x);
+  const tc::Tc5 t5 = tc_setup(dsm, ColGeom<N>::SMEM + T * kVals, (int)threadIdx.x, (int)blockDim.x);
   body_zconv<N, false, TCM>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, W, (int)blockIdx.x, (int)blockIdx.y,
-                            (int)threadIdx.x, dsm, stash, T, tcx);
+                            (int)threadIdx.x, dsm, stash, T, TcCtx{&t5});
+  tc::tc5_teardown(t5, (int)threadIdx.x, (int)blockDim.x);
 }
 
 // opt the kernel in to more than 48 KiB of dynamic shared memory where it needs it
@@ -94,7 +99,7 @@ cudaError_t FC_TC_NAME(tc_x_r2c, FC_TC_SUFFIX)(const float* in, long long in_pit
 #define FC_CASE(n_)                                                                                             \
   case n_: {                                                                                                    \
     using G = fast::RowGeom<n_>;                                                                                \
-    const size_t sm = sizeof(float2) * G::SMEM + fast::tc_bytes(G::THREADS);                                    \
+    const size_t sm = fast::tc_smem(G::SMEM, G::THREADS);                                    \
     const dim3 grid((unsigned)G::tiles(nrows));                                                                 \
     cudaError_t e;                                                                                              \
     if (taps) {                                                                                                 \
@@ -124,7 +129,7 @@ cudaError_t FC_TC_NAME(tc_x_c2r, FC_TC_SUFFIX)(const float2* in, long long in_pi
 #define FC_CASE(n_)                                                                                  \
   case n_: {                                                                                         \
     using G = fast::RowGeom<n_>;                                                                     \
-    const size_t sm = sizeof(float2) * G::SMEM + fast::tc_bytes(G::THREADS);                         \
+    const size_t sm = fast::tc_smem(G::SMEM, G::THREADS);                         \
     const dim3 grid((unsigned)G::tiles(nrows));                                                      \
     const cudaError_t e = fast::allow_smem(fast::k_c2r_tc<n_>, sm);            \
     if (e != cudaSuccess) return e;                                                                  \
@@ -147,7 +152,7 @@ cudaError_t FC_TC_NAME(tc_cols, FC_TC_SUFFIX)(int mode, const float2* src, long 
 #define FC_CASE(n_)                                                                                              \
   case n_: {                                                                                                     \
     using G = fast::ColGeom<n_>;                                                                                 \
-    const size_t sm = sizeof(float2) * G::SMEM + fast::tc_bytes(G::THREADS);                                     \
+    const size_t sm = fast::tc_smem(G::SMEM, G::THREADS);                                     \
     const dim3 grid((ncols + G::B - 1) / G::B, nplanes);                                                         \
     cudaError_t e;                                                                                               \
     if (mode == 2) {                                                                                             \
@@ -182,7 +187,7 @@ cudaError_t FC_TC_NAME(tc_zconv, FC_TC_SUFFIX)(float2* S, const float2* KXY, lon
 #define FC_CASE(n_)                                                                                              \
   case n_: {                                                                                                     \
     using G = fast::ColGeom<n_>;                                                                                 \
-    const size_t sm = sizeof(float2) * (G::SMEM + G::THREADS * fast::kVals) + fast::tc_bytes(G::THREADS);        \
+    const size_t sm = fast::tc_smem(G::SMEM + G::THREADS * fast::kVals, G::THREADS);        \
     const dim3 grid((ncols + G::B - 1) / G::B, ny);                                                              \
     const cudaError_t e = fast::allow_smem(fast::k_zconv_tc<n_>, sm);                      \
     if (e != cudaSuccess) return e;                                                                              \
@@ -194,6 +199,14 @@ cudaError_t FC_TC_NAME(tc_zconv, FC_TC_SUFFIX)(float2* S, const float2* KXY, lon
     default:
       return cudaErrorNotSupported;
   }
+}
+
+cudaError_t FC_TC_NAME(tc_timeouts_read_async, FC_TC_SUFFIX)(unsigned int* dst, cudaStream_t st) {
+  return cudaMemcpyFromSymbolAsync(dst, tc::g_tc5_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
+}
+void FC_TC_NAME(tc_timeouts_clear, FC_TC_SUFFIX)() {
+  const unsigned int zero = 0;
+  cudaMemcpyToSymbol(tc::g_tc5_timeouts, &zero, sizeof(zero));
 }
 
 }  // namespace fc
