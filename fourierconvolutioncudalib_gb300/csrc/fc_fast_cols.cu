@@ -89,9 +89,34 @@ bool fast_cols_supported(int n) {
   }
 }
 
+namespace fast {
+// the persistent tensor-map y pass, for in-place passes over a spectrum whose
+// planes are ny rows apart (ps == es * n); *used false: not selected or not applicable
+template <bool INV>
+static cudaError_t dispatch_cols_pipe(int n, float2* S, long long ps, long long es, int ncols, int nplanes,
+                                      const float2* W, cudaStream_t st, bool* used) {
+  *used = false;
+  switch (n) {
+#define FC_CASE(n_) \
+  case n_:          \
+    return cols_pipe_launch<n_, INV>(S, ps, es, ncols, nplanes, W, st, used);
+    FC_COL_SIZES(FC_CASE)
+#undef FC_CASE
+    default:
+      return cudaSuccess;
+  }
+}
+}  // namespace fast
+
 cudaError_t fast_cols(const float2* src, float2* dst, long long ps, long long es, int ncols, int nplanes, bool inverse,
                       const FcAxis& ax, cudaStream_t st) {
   if (nplanes <= 0 || ncols <= 0) return cudaSuccess;
+  if (src == dst) {
+    bool used = false;
+    const cudaError_t e = inverse ? fast::dispatch_cols_pipe<true>(ax.n, dst, ps, es, ncols, nplanes, ax.W, st, &used)
+                                  : fast::dispatch_cols_pipe<false>(ax.n, dst, ps, es, ncols, nplanes, ax.W, st, &used);
+    if (e != cudaSuccess || used) return e;
+  }
   const ColPlain s{src, ps, es};
   return inverse ? fast::dispatch_cols<true>(ax.n, s, dst, ps, es, ncols, nplanes, ax.W, st)
                  : fast::dispatch_cols<false>(ax.n, s, dst, ps, es, ncols, nplanes, ax.W, st);
@@ -143,6 +168,12 @@ bool fast_cols_wide_supported(int n) {
 cudaError_t fast_cols_wide(float2* S, long long ps, long long es, int ncols, int nplanes, bool inverse,
                            const FcAxis& ax, cudaStream_t st) {
   if (nplanes <= 0 || ncols <= 0) return cudaSuccess;
+  {
+    bool used = false;
+    const cudaError_t e = inverse ? fast::dispatch_cols_pipe<true>(ax.n, S, ps, es, ncols, nplanes, ax.W, st, &used)
+                                  : fast::dispatch_cols_pipe<false>(ax.n, S, ps, es, ncols, nplanes, ax.W, st, &used);
+    if (e != cudaSuccess || used) return e;
+  }
   switch (ax.n) {
 #define FC_CASE(n_)                                                                      \
   case n_:                                                                               \
@@ -177,5 +208,14 @@ cudaError_t fast_cols_kx(const float2* kx_spec, long long pitch, int krows, int 
   const ColKX s{kx_spec, pitch, krows, hy, ax.n};
   return fast::dispatch_cols<false>(ax.n, s, dst, (long long)ax.n * pitch, pitch, ncols, nplanes, ax.W, st);
 }
+
+cudaError_t ycols_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
+  return cudaMemcpyFromSymbolAsync(dst, fast::g_ypipe_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
+}
+void ycols_timeouts_clear() {
+  const unsigned int zero = 0;
+  cudaMemcpyToSymbol(fast::g_ypipe_timeouts, &zero, sizeof(zero));
+}
+cudaError_t ycols_wait_ctl_set(long long limit, int skip_copies) { return async::wait_ctl_set_tu(limit, skip_copies); }
 
 }  // namespace fc

@@ -44,6 +44,14 @@ using ColGeom = ColGeomB<N, 32>;
 template <int N>
 using ColGeomWide = ColGeomB<N, 32, 512, 8192>;
 
+// rows per tensor-map box of a column of N values: the largest divisor of N of
+// at most 256 (a box dimension is at most 256, and equal boxes cover N exactly)
+constexpr int zbox_rows(int n) {
+  int nb = (n + 255) / 256;
+  while (n % nb) ++nb;
+  return n / nb;
+}
+
 // y pass body: tile (bx, plane) = columns [bx*B, bx*B + B) of one plane.
 // REV: radix order of the transform (a standalone pass may run the inverse in
 // the forward order, which exchanges with fewer shared-memory bank conflicts)
@@ -91,6 +99,159 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* d
                                                       (int)threadIdx.x, sm);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent in-place y pass on tensor-map tiles (opt-in, FC_YPIPE=1).  The
+// spectrum S is [nz][ny][pitch]; a tile is B adjacent columns of one plane,
+// all N = ny rows.  Each CTA walks the tiles with a stride of the grid size; a
+// tile arrives in shared memory (ISTAGE, rows of B columns) by tensor-map
+// copies of YBOX rows each, and the copy of the CTA's next tile is issued as
+// soon as every thread has read the current one into registers, so it lands
+// behind the current tile's transform and stores.  The stage tables of the
+// radix chain sit in shared memory.  Every box starts 128-byte aligned
+// (lengths that fail it keep k_cols); waits are bounded as in the fused z
+// pass.
+template <int N>
+struct YPipe {
+  using G = ColGeom<N>;
+  static constexpr int B = G::B;
+  static constexpr int THREADS = G::THREADS;
+  static constexpr int XCH_BYTES = ((G::SMEM * (int)sizeof(float2) + 127) / 128) * 128;
+  static constexpr int YBOX = zbox_rows(N);
+  static constexpr int NBOX = N / YBOX;
+  static constexpr int IBYTES = N * B * (int)sizeof(float2);
+  static constexpr int ISTAGE_OFF = XCH_BYTES;
+  static constexpr int TWN = Plan<N>::tab_size(false);
+  static constexpr int TW_OFF = ISTAGE_OFF + ((IBYTES + 127) / 128) * 128;
+  static constexpr int BAR_OFF = TW_OFF + ((TWN * (int)sizeof(float2) + 127) / 128) * 128;
+  static constexpr int SMEM_BYTES = BAR_OFF + 128;
+  static_assert(YBOX <= 256 && YBOX * NBOX == N, "boxes must tile the column");
+  static constexpr bool OK = (YBOX * B * (int)sizeof(float2)) % 128 == 0 && (B * (int)sizeof(float2)) % 16 == 0 &&
+                             SMEM_BYTES <= 227 * 1024;
+};
+
+// expired waits of the persistent y pass (per translation unit)
+[[maybe_unused]] static __device__ unsigned int g_ypipe_timeouts;
+
+template <int N, bool INV>
+__global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restrict__ S, long long ps, long long es,
+                                                                  int ncols, int nplanes, const float2* __restrict__ W,
+                                                                  const __grid_constant__ CUtensorMap map) {
+  using P = YPipe<N>;
+  constexpr int B = P::B;
+  constexpr int R0 = first_radix<N, false>(), RF = last_radix<N, false>();
+  extern __shared__ __align__(128) unsigned char ypsm[];
+  float2* xch = reinterpret_cast<float2*>(ypsm);
+  float2* ist = reinterpret_cast<float2*>(ypsm + P::ISTAGE_OFF);
+  float2* tws = reinterpret_cast<float2*>(ypsm + P::TW_OFF);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(ypsm + P::BAR_OFF);
+  const int tid = (int)threadIdx.x;
+  const int c = tid % B;
+  const int t = tid / B;
+  const int ntx = (ncols + B - 1) / B;
+  const int ntiles = ntx * nplanes;  // tile counts fit an int for every supported shape
+  const bool skip = async::copies_skipped();
+  async::pdl_launch_dependents();
+  auto issue = [&](int ti) {
+    const int bx = ti % ntx, plane = ti / ntx;
+    async::bar_expect(bar, (unsigned)P::IBYTES);
+    if (!skip)
+#pragma unroll
+      for (int b = 0; b < P::NBOX; ++b)
+        async::tensor_load_3d(ist + b * P::YBOX * B, &map, bx * B, b * P::YBOX, plane, bar);
+  };
+  copy_stage_tables<N, false>(tws, W, tid, P::THREADS);  // the twiddle tables are not written by any pass
+  if (tid == 0) {
+    async::bar_init(bar, 1);
+    async::bar_init_fence();
+  }
+  __syncthreads();
+  async::pdl_wait();  // the previous pass's output is complete and visible
+  int ti = (int)blockIdx.x;
+  if (tid == 0 && ti < ntiles) issue(ti);
+  bool pend = ti < ntiles;
+  bool expired = false;
+  uint32_t ph = 0;
+  const ColLay<B> lay{xch, c};
+  for (; ti < ntiles; ti += (int)gridDim.x, ph ^= 1u) {
+    const int plane = ti / ntx;
+    const int col = (ti % ntx) * B + c;
+    const bool ok = col < ncols && t < P::G::T;
+    float2 v[kVals];
+    if (!__syncthreads_and(async::bar_wait(bar, ph))) {
+      expired = true;
+      break;
+    }
+    pend = false;
+#pragma unroll
+    for (int q = 0; q < kVals; ++q) {
+      const int j = stage_pos<N, R0>(t, q);
+      v[q] = (ok && j >= 0) ? ist[j * B + c] : make_float2(0.f, 0.f);
+    }
+    async::proxy_fence();
+    __syncthreads();  // every thread has read ISTAGE
+    if (ti + (int)gridDim.x < ntiles) {
+      if (tid == 0) issue(ti + (int)gridDim.x);
+      pend = true;
+    }
+    fft<N, INV, tc::kNone, false, true>(v, lay, t, tws);
+    if (ok) {
+      float2* d = S + (long long)plane * ps + col;
+#pragma unroll
+      for (int q = 0; q < kVals; ++q) {
+        const int j = stage_pos<N, RF>(t, q);
+        if (j >= 0) d[(long long)j * es] = v[q];
+      }
+    }
+  }
+  if (expired) {
+    if (tid == 0) atomicAdd(&g_ypipe_timeouts, 1u);
+    if (pend) (void)async::bar_wait(bar, ph);
+  }
+}
+
+// Host: encode a 3-D tensor map of a spectrum of ncols columns (row pitch
+// `pitch` float2), ny rows and nz planes, box bx x by x bz elements of 8
+// bytes; false when the driver entry point is missing or a rule is broken.
+bool tile_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int nz, int bx, int by,
+                     int bz);
+// FC_YPIPE=1 selects the persistent tensor-map y passes (off by default: on
+// GB300 they measured no faster than the one-tile-per-CTA passes, which also
+// leave SMs to the kernel-spectrum passes running beside the image y pass)
+bool ypipe_enabled();
+
+// Host: launch the persistent in-place y pass when selected and its geometry applies (sets *used)
+template <int N, bool INV>
+static cudaError_t cols_pipe_launch(float2* S, long long ps, long long es, int ncols, int nplanes, const float2* W,
+                                    cudaStream_t st, bool* used) {
+  using P = YPipe<N>;
+  *used = false;
+  if constexpr (!P::OK) {
+    return cudaSuccess;
+  } else {
+    if (!ypipe_enabled() || ncols < 1 || nplanes < 1 || ps != es * N) return cudaSuccess;
+    CUtensorMap map;
+    if (!tile_tensor_map(&map, S, es, N, ncols, nplanes, P::B, P::YBOX, 1)) return cudaSuccess;
+    auto kern = k_cols_pipe<N, INV>;
+    static int s_occ = 0;  // resident CTAs per SM of this instantiation (a benign race: same value)
+    int occ = s_occ;
+    if (occ == 0) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, P::THREADS, P::SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      if (occ < 1) return cudaSuccess;
+      s_occ = occ;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long ntiles = (long long)((ncols + P::B - 1) / P::B) * nplanes;
+    const long long grid = std::min<long long>(ntiles, (long long)occ * sms);
+    *used = true;
+    return async::launch_pdl(kern, (unsigned)grid, P::THREADS, P::SMEM_BYTES, st, S, ps, es, ncols, nplanes, W, map);
+  }
+}
+
 // Fused z pass.  Kernel plane p of KXY holds z = (p - hz) mod nz.  The
 // kernel column is transformed first and parked in a per-thread private
 // shared-memory stash (stash[q*nstash + tid], no barrier needed), so only one
@@ -107,13 +268,6 @@ using ZTile = ColGeomB<N, 16>;
 // chain and its inverse the forward chain (either pairing hands the spectrum
 // over in registers; this one measured 0.4-2 % faster on GB300)
 constexpr bool kZRev = true;
-// z rows per tensor-map box of the image stage: the largest divisor of N of at
-// most 256 (a box dimension is at most 256, and equal boxes cover N exactly)
-constexpr int zbox_rows(int n) {
-  int nb = (n + 255) / 256;
-  while (n % nb) ++nb;
-  return n / nb;
-}
 template <int N>
 struct ZGeom {
   // exchange tile, stash, image stage buffer, mbarrier (float2 elements); the

@@ -52,6 +52,29 @@ bool zstage_use_tma() {
   return on;
 }
 
+bool tile_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int nz, int bx, int by,
+                     int bz) {
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode || ((uintptr_t)S & 15) != 0 || (pitch * (long long)sizeof(float2)) % 16 != 0 || bx < 1 || by < 1 ||
+      bz < 1 || bx > 256 || by > 256 || bz > 256 || (bx * sizeof(float2)) % 16 != 0 || ncols < 1 || ny < 1 || nz < 1)
+    return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)pitch * sizeof(float2), (cuuint64_t)pitch * sizeof(float2) * ny};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<float2*>(S), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool ypipe_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("FC_YPIPE");
+    return e && std::atoi(e) != 0;
+  }();
+  return on;
+}
+
 bool zpipe_enabled() {
   static const bool on = [] {
     const char* e = std::getenv("FC_ZPIPE");

@@ -1079,14 +1079,18 @@ static void enqueue_timeout_reads(DevCtx& c, cudaStream_t st) {
   cuda_check(zadj_timeouts_read_async(c.h_timeouts + 2, st), "timeout count read");
   cuda_check(tc_timeouts_read_async_fp16(c.h_timeouts + 3, st), "timeout count read");
   cuda_check(tc_timeouts_read_async_bf16(c.h_timeouts + 4, st), "timeout count read");
+  cuda_check(ycols_timeouts_read_async(c.h_timeouts + 5, st), "timeout count read");
 }
 static void check_device_timeouts(DevCtx& c) {
-  if (!(c.h_timeouts[0] | c.h_timeouts[1] | c.h_timeouts[2] | c.h_timeouts[3] | c.h_timeouts[4])) return;
+  if (!(c.h_timeouts[0] | c.h_timeouts[1] | c.h_timeouts[2] | c.h_timeouts[3] | c.h_timeouts[4] |
+        c.h_timeouts[5]))
+    return;
   pipe_timeouts_clear();
   zconv_timeouts_clear();
   zadj_timeouts_clear();
   tc_timeouts_clear_fp16();
   tc_timeouts_clear_bf16();
+  ycols_timeouts_clear();
   FC_THROW(FC_ERR_TIMEOUT, "a bounded device wait expired in an asynchronous copy");
 }
 
@@ -1810,6 +1814,7 @@ int fc_test_set_wait_fault(long long limit_cycles, int skip_copies) {
     cuda_check(pipe_wait_ctl_set(limit_cycles, skip_copies), "wait control (x passes)");
     cuda_check(zconv_wait_ctl_set(limit_cycles, skip_copies), "wait control (fused z pass)");
     cuda_check(zadj_wait_ctl_set(limit_cycles, skip_copies), "wait control (adjoint z pass)");
+    cuda_check(ycols_wait_ctl_set(limit_cycles, skip_copies), "wait control (y passes)");
   });
 }
 

@@ -135,6 +135,10 @@ void zadj_timeouts_clear();
 cudaError_t pipe_wait_ctl_set(long long limit, int skip_copies);
 cudaError_t zconv_wait_ctl_set(long long limit, int skip_copies);
 cudaError_t zadj_wait_ctl_set(long long limit, int skip_copies);
+// the persistent tensor-map y passes (fc_fast_cols.cu, selected by FC_YPIPE=1)
+cudaError_t ycols_timeouts_read_async(unsigned int* dst, cudaStream_t st);
+void ycols_timeouts_clear();
+cudaError_t ycols_wait_ctl_set(long long limit, int skip_copies);
 // resolve the tensor-map encoder of the fused z pass's stage copy (host; call
 // outside stream capture, e.g. when a device context is created)
 void zstage_prepare();

@@ -2,10 +2,10 @@
 
 The library picks, per pass, a persistent kernel whose tiles arrive by
 asynchronous copies (x passes: bulk copies; fused z pass: tensor-map copies of
-the image tile and of the kernel planes) with programmatic dependent launch,
-or a one-tile-per-CTA kernel.  The selection is read from the environment once
-per process (FC_PIPE, FC_ZPIPE, FC_PDL), so each variant runs in a child
-process.  Tolerance: rel-L2 <= 1e-5 and max-abs <= 1e-5 * max against the FP64
+the image tile and of the kernel planes; y passes, when selected: tensor-map
+copies) with programmatic dependent launch, or a one-tile-per-CTA kernel.  The
+selection is read from the environment once per process (FC_PIPE, FC_YPIPE,
+FC_ZPIPE, FC_PDL), so each variant runs in a child process.  Tolerance: rel-L2 <= 1e-5 and max-abs <= 1e-5 * max against the FP64
 oracle, on shapes that include columns longer than 256 (z = 300, 512, 1024:
 the tensor-map stage in two or four boxes).
 """
@@ -43,8 +43,9 @@ print("ok")
 """
 
 
-@pytest.mark.parametrize("env", [{}, {"FC_ZPIPE": "0"}, {"FC_PDL": "0"}, {"FC_PIPE": "0", "FC_PDL": "0"}],
-                         ids=["default", "z-one-tile-per-cta", "no-pdl", "x-one-tile-per-cta"])
+@pytest.mark.parametrize("env", [{}, {"FC_YPIPE": "1"}, {"FC_ZPIPE": "0"}, {"FC_PDL": "0"},
+                                 {"FC_PIPE": "0", "FC_PDL": "0", "FC_YPIPE": "1"}],
+                         ids=["default", "y-tensor-map", "z-one-tile-per-cta", "no-pdl", "x-one-tile-per-cta"])
 def test_pass_kernel_variants(cuda, fclib, env):
     e = dict(os.environ)
     e.update(env)
