@@ -1,7 +1,10 @@
 #!/usr/bin/env bash
 # Compile the reference library (FourierConvolutionCUDALib) from its own,
 # unmodified sources into oracle/_ref/libfc_reference.so, for the parity tests
-# and the timing of the reference's GPU build on the same GPU.
+# and the timing of the reference's GPU build on the same GPU; and, into
+# oracle/_ref/libfc_reference_sub.so, the host driver oracle/ref_subsampled.cu
+# of the reference's subsampled-kernel product, compiled together with the
+# reference's convolution3Dfft.cu.
 #
 # The reference's CMake cannot be used (it relies on the removed FindCUDA
 # module and on pre-Turing architectures), so nvcc is called on its two .cu
@@ -36,7 +39,9 @@ done
 LIB="$OUT/libfc_reference.so"
 ARCHTAG="$OUT/.built_for"
 # rebuild when a source is newer, or when the library was built on another host architecture
-if [ -f "$LIB" ] && [ -f "$ARCHTAG" ] && [ "$(cat "$ARCHTAG")" = "$(uname -m)" ] && \
+SUBLIB="$OUT/libfc_reference_sub.so"
+if [ -f "$LIB" ] && [ -f "$SUBLIB" ] && [ -f "$ARCHTAG" ] && [ "$(cat "$ARCHTAG")" = "$(uname -m)" ] && \
+   [ -z "$(find "$SRC" "$HERE/ref_subsampled.cu" -newer "$SUBLIB" -type f)" ] && \
    [ -z "$(find "$SRC" -newer "$LIB" -type f)" ]; then
   echo "$LIB"
   exit 0
@@ -49,8 +54,16 @@ FLAGS=(-std=c++17 -O2 --use_fast_math -Xcompiler -fPIC -gencode arch=compute_103
 p1=$!
 "$NVCC" "${FLAGS[@]}" -c "$SRC/standardCUDAfunctions.cu" -o "$OUT/standardCUDAfunctions.o" &
 p2=$!
+# the host driver of the reference's subsampled-kernel product (oracle/ref_subsampled.cu), which
+# includes the reference's convolution3Dfft.cu, as a library of its own
+"$NVCC" "${FLAGS[@]}" -c "$HERE/ref_subsampled.cu" -o "$OUT/ref_subsampled.o" &
+p3=$!
 wait $p1
 wait $p2
+wait $p3
+"$NVCC" -shared -gencode arch=compute_103a,code=sm_103a -Xlinker -soname=libfc_reference_sub.so \
+  -Xlinker -rpath=/usr/local/cuda/lib64 -o "$SUBLIB.tmp" "$OUT/ref_subsampled.o" -lcufft -lcuda
+mv "$SUBLIB.tmp" "$SUBLIB"
 "$NVCC" -shared -gencode arch=compute_103a,code=sm_103a -Xlinker -soname=libfc_reference.so -Xlinker -rpath=/usr/local/cuda/lib64 -o "$LIB.tmp" \
   "$OUT/convolution3Dfft.o" "$OUT/standardCUDAfunctions.o" -lcufft -lcuda
 mv "$LIB.tmp" "$LIB"

@@ -37,6 +37,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
 LIB = REF_DIR / "libfc_reference.so"
+SUBLIB = REF_DIR / "libfc_reference_sub.so"
 
 
 def build() -> Optional[Path]:
@@ -50,7 +51,7 @@ def build() -> Optional[Path]:
 def library_path() -> Optional[Path]:
     """The built library when it was built for this host's architecture."""
     tag = REF_DIR / ".built_for"
-    if LIB.exists() and tag.exists() and tag.read_text().strip() == platform.machine():
+    if LIB.exists() and SUBLIB.exists() and tag.exists() and tag.read_text().strip() == platform.machine():
         return LIB
     return None
 
@@ -114,6 +115,16 @@ def time_inplace(image: np.ndarray, kernel: np.ndarray, reps: int, warmup: int =
                      {"im0": np.ascontiguousarray(image, np.float32), "k0": np.ascontiguousarray(kernel, np.float32)},
                      timeout=1800.0)
     return {"seconds": [float(s) for s in out["seconds"]], "output": out["out0"]}
+
+
+def subsampled(image: np.ndarray, kernel: np.ndarray, device: int = 0) -> np.ndarray:
+    """The reference's subsampled-kernel product (modulateAndNormalizeSubsampled_kernel,
+    src/convolution3Dfft.cu:65-125) driven by oracle/ref_subsampled.cu: cuFFT R2C of
+    the image and of the kernel at their own sizes, the reference's kernel,
+    cuFFT C2R.  image [nz][ny][nx], kernel [kz][ky][kx]."""
+    out = _run_child({"op": "subsampled", "device": device},
+                     {"im0": np.ascontiguousarray(image, np.float32), "k0": np.ascontiguousarray(kernel, np.float32)})
+    return out["out0"]
 
 
 def device_queries(device: int = 0) -> dict:
@@ -187,6 +198,19 @@ def _child(spec: dict) -> None:
         p = L.convolution3DfftCUDA(im.ctypes.data_as(FP), IA(*im.shape), k.ctypes.data_as(FP), IA(*k.shape), dev)
         res = np.ctypeslib.as_array(p, shape=(im.size,)).reshape(im.shape).copy()
         out["out0"] = res  # the new[] buffer is left to the process exit
+    elif op == "subsampled":
+        S = ctypes.CDLL(str(Path(spec["lib"]).parent / "libfc_reference_sub.so"), mode=ctypes.RTLD_LOCAL)
+        S.fcref_subsampled.restype = ctypes.c_int
+        S.fcref_subsampled.argtypes = [FP, ctypes.c_int, ctypes.c_int, ctypes.c_int, FP, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, FP, ctypes.c_int]
+        im = np.ascontiguousarray(arrays["im0"], np.float32)
+        k = np.ascontiguousarray(arrays["k0"], np.float32)
+        res = np.empty_like(im)
+        rc = S.fcref_subsampled(im.ctypes.data_as(FP), *im.shape, k.ctypes.data_as(FP), *k.shape,
+                                res.ctypes.data_as(FP), dev)
+        if rc != 0:
+            raise RuntimeError(f"fcref_subsampled failed with code {rc}")
+        out["out0"] = res
     elif op == "queries":
         n = L.getNumDevicesCUDA()  # initialises the runtime (and the driver) first
         name = ctypes.create_string_buffer(256)

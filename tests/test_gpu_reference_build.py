@@ -14,6 +14,8 @@ run in a child process (oracle/reference_gpu.py).  Cases:
   * the reference's convolution3DfftCUDA (src/convolution3Dfft.cu:299-391),
     whose packed input is transformed as if it had the padded in-place layout,
     against the FP64 oracle;
+  * the subsampled-kernel variant against the reference's own device product
+    (src/convolution3Dfft.cu:65-125, driven by oracle/ref_subsampled.cu);
   * the device-query exports.
 
 Tolerance: rel-L2 <= 1e-5 and max-abs <= 1e-5 * max|reference output|; the
@@ -167,6 +169,33 @@ def test_reference_noninplace_entry_layout(refgpu, orc):
     dims = (64, 64, 64)
     ours = fc.convolution3DfftCUDA(np.ascontiguousarray(im), dims, k, (7, 7, 7), 0)
     _check(ours, exact, "ours convolution3DfftCUDA vs FP64")
+
+
+@pytest.mark.parametrize("shape,kshape", [((64, 128, 128), (16, 10, 12)), ((128, 512, 512), (62, 31, 30)),
+                                          ((96, 64, 256), (15, 9, 24))])
+def test_subsampled_matches_reference_product(refgpu, orc, shape, kshape):
+    """convolution3DfftCUDAInPlaceSaveMemory against the reference's own
+    subsampled-kernel product (modulateAndNormalizeSubsampled_kernel,
+    src/convolution3Dfft.cu:65-125) driven on cuFFT by oracle/ref_subsampled.cu,
+    and both against the FP64 restatement.  Image extents are powers of two, so
+    the ratio k/n is exact in float32 under the reference's fast-math division
+    and the nearest-coefficient indices agree; kernel x extents are even, where
+    the reference reads inside its half-spectrum rows (for odd ones it reads one
+    coefficient past a row at the x Nyquist, where this library takes the
+    Hermitian mirror)."""
+    rng = np.random.Generator(np.random.PCG64(sum(shape)))
+    im = rng.random(shape).astype(np.float32)
+    k = _gauss(kshape, (kshape[0] / 6, kshape[1] / 6, kshape[2] / 6))
+    ref = refgpu.subsampled(im, k)
+    ours = np.ascontiguousarray(im).copy()
+    nz, ny, nx = shape
+    kz, ky, kx = kshape
+    fc.convolution3DfftCUDAInPlaceSaveMemory(ours, (nx, ny, nz), k, (kx, ky, kz), 0)
+    exact = orc.subsampled_fp64(im, k)
+    rr, rm = _cmp(ref, exact)
+    print(f"{shape} {kshape}: reference product vs FP64 restatement rel-L2 {rr:.3e} max {rm:.3e}")
+    _check(ours, ref, f"{shape} {kshape} ours vs reference subsampled product")
+    _check(ours, exact, f"{shape} {kshape} ours vs FP64 restatement")
 
 
 def test_device_queries_match_reference_build(refgpu, fclib):
