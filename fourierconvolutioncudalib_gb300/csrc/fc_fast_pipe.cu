@@ -24,9 +24,6 @@ struct PipeRows {
   using G = RowGeom<N>;
   static constexpr int ROWS = 2 * G::LPB;
   static constexpr int XBYTES = ((G::SMEM * (int)sizeof(float2) + 127) / 128) * 128;  // exchange area
-  // stage tables of the chain both passes run (REV = false), copied into shared memory
-  static constexpr int TWN = Plan<N>::tab_size(false);
-  static constexpr int TWBYTES = ((TWN * (int)sizeof(float2) + 127) / 128) * 128;
 };
 
 // rows of the tile in shared memory: element x of global row r is b[(r - row0) * pitch + x]
@@ -46,13 +43,11 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
   extern __shared__ __align__(128) unsigned char dsm[];
   __shared__ uint64_t bar;
   float2* sm = reinterpret_cast<float2*>(dsm);
-  float2* tws = reinterpret_cast<float2*>(dsm + P::XBYTES);
-  unsigned char* buf = dsm + P::XBYTES + P::TWBYTES;
+  unsigned char* buf = dsm + P::XBYTES;
   const int tid = (int)threadIdx.x;
   const long long ntiles = RowGeom<N>::tiles(nrows);
   const long long row_bytes = in_pitch * (C2R ? (long long)sizeof(float2) : (long long)sizeof(float));
   async::pdl_launch_dependents();
-  copy_stage_tables<N, false>(tws, W, tid, RowGeom<N>::THREADS);  // the twiddle tables are not written by any pass
   if (tid == 0) {
     async::bar_init(&bar, 1);
     async::bar_init_fence();
@@ -89,9 +84,9 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
       issue(tile + gridDim.x);
     }
     if constexpr (C2R)
-      finish_c2r<N, tc::kNone, false, true>(v, s, reinterpret_cast<float*>(out), out_pitch, tws, sm);
+      finish_c2r<N, tc::kNone, false>(v, s, reinterpret_cast<float*>(out), out_pitch, W, sm);
     else
-      finish_r2c<N, tc::kNone, false, true>(v, s, reinterpret_cast<float2*>(out), out_pitch, tws, sm);
+      finish_r2c<N>(v, s, reinterpret_cast<float2*>(out), out_pitch, W, sm);
   }
 }
 
@@ -101,7 +96,7 @@ static cudaError_t run_rows_pipe(const void* in, long long in_pitch, void* out, 
   using P = PipeRows<N>;
   using G = RowGeom<N>;
   const size_t buf_bytes = (size_t)P::ROWS * in_pitch * (C2R ? sizeof(float2) : sizeof(float));
-  const size_t smem = P::XBYTES + P::TWBYTES + buf_bytes;
+  const size_t smem = P::XBYTES + buf_bytes;
   auto kern = k_rows_pipe<N, C2R>;
   // (dynamic bytes << 8 | resident CTAs per SM) of the last launch configuration
   static std::atomic<long long> s_occ{0};
