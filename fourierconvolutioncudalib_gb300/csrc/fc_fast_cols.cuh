@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* d
 }
 
 // ---------------------------------------------------------------------------
-// Persistent in-place y pass on tensor-map tiles (opt-in, FC_YPIPE=1).  The
+// Persistent in-place y pass on tensor-map tiles (default for power-of-two lengths >= 512).  The
 // spectrum S is [nz][ny][pitch]; a tile is B adjacent columns of one plane,
 // all N = ny rows.  Each CTA walks the tiles with a stride of the grid size; a
 // tile arrives in shared memory (ISTAGE, rows of B columns) by tensor-map
@@ -214,10 +214,10 @@ __global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restr
 // bytes; false when the driver entry point is missing or a rule is broken.
 bool tile_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny, int ncols, int nz, int bx, int by,
                      int bz);
-// FC_YPIPE=1 selects the persistent tensor-map y passes (off by default: on
-// GB300 they measured no faster than the one-tile-per-CTA passes, which also
-// leave SMs to the kernel-spectrum passes running beside the image y pass)
-bool ypipe_enabled();
+// Whether the persistent tensor-map y pass runs for columns of length n: by
+// default for power-of-two lengths from 512 (the one-tile-per-CTA pass is
+// faster below); FC_YPIPE=0 never, FC_YPIPE=1 wherever its geometry applies
+bool ypipe_selected(int n);
 
 // Host: launch the persistent in-place y pass when selected and its geometry applies (sets *used)
 template <int N, bool INV>
@@ -228,7 +228,7 @@ static cudaError_t cols_pipe_launch(float2* S, long long ps, long long es, int n
   if constexpr (!P::OK) {
     return cudaSuccess;
   } else {
-    if (!ypipe_enabled() || ncols < 1 || nplanes < 1 || ps != es * N) return cudaSuccess;
+    if (!ypipe_selected(N) || ncols < 1 || nplanes < 1 || ps != es * N) return cudaSuccess;
     CUtensorMap map;
     if (!tile_tensor_map(&map, S, es, N, ncols, nplanes, P::B, P::YBOX, 1)) return cudaSuccess;
     auto kern = k_cols_pipe<N, INV>;

@@ -67,12 +67,17 @@ bool tile_tensor_map(CUtensorMap* map, const float2* S, long long pitch, int ny,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-bool ypipe_enabled() {
-  static const bool on = [] {
+bool ypipe_selected(int n) {
+  // -1: by length (unset), 0: never (FC_YPIPE=0), 1: every length it applies to (FC_YPIPE=1)
+  static const int mode = [] {
     const char* e = std::getenv("FC_YPIPE");
-    return e && std::atoi(e) != 0;
+    return e ? (std::atoi(e) != 0 ? 1 : 0) : -1;
   }();
-  return on;
+  if (mode >= 0) return mode == 1;
+  // measured on GB300 over whole convolutions: faster at 512 and 1024
+  // (512x512x128: 0.308 against 0.315 ms; 1024x1024x256: 2.356 against
+  // 2.400 ms), slower at 448 (0.225 against 0.218 ms)
+  return n >= 512 && (n & (n - 1)) == 0;
 }
 
 bool zpipe_enabled() {

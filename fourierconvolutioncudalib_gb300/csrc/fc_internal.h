@@ -135,7 +135,7 @@ void zadj_timeouts_clear();
 cudaError_t pipe_wait_ctl_set(long long limit, int skip_copies);
 cudaError_t zconv_wait_ctl_set(long long limit, int skip_copies);
 cudaError_t zadj_wait_ctl_set(long long limit, int skip_copies);
-// the persistent tensor-map y passes (fc_fast_cols.cu, selected by FC_YPIPE=1)
+// the persistent tensor-map y passes (fc_fast_cols.cu; power-of-two lengths >= 512, FC_YPIPE=0/1 overrides)
 cudaError_t ycols_timeouts_read_async(unsigned int* dst, cudaStream_t st);
 void ycols_timeouts_clear();
 cudaError_t ycols_wait_ctl_set(long long limit, int skip_copies);

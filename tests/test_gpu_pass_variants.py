@@ -43,9 +43,10 @@ print("ok")
 """
 
 
-@pytest.mark.parametrize("env", [{}, {"FC_YPIPE": "1"}, {"FC_ZPIPE": "0"}, {"FC_PDL": "0"},
+@pytest.mark.parametrize("env", [{}, {"FC_YPIPE": "1"}, {"FC_YPIPE": "0"}, {"FC_ZPIPE": "0"}, {"FC_PDL": "0"},
                                  {"FC_PIPE": "0", "FC_PDL": "0", "FC_YPIPE": "1"}],
-                         ids=["default", "y-tensor-map", "z-one-tile-per-cta", "no-pdl", "x-one-tile-per-cta"])
+                         ids=["default", "y-tensor-map-all", "y-one-tile-per-cta", "z-one-tile-per-cta", "no-pdl",
+                              "x-one-tile-per-cta"])
 def test_pass_kernel_variants(cuda, fclib, env):
     e = dict(os.environ)
     e.update(env)

@@ -15,7 +15,8 @@ run in a child process (oracle/reference_gpu.py).  Cases:
     whose packed input is transformed as if it had the padded in-place layout,
     against the FP64 oracle;
   * the subsampled-kernel variant against the reference's own device product
-    (src/convolution3Dfft.cu:65-125, driven by oracle/ref_subsampled.cu);
+    (src/convolution3Dfft.cu:65-125, driven by oracle/ref_subsampled.cu), on
+    every x frequency but DC and Nyquist, where that product is not Hermitian;
   * the device-query exports.
 
 Tolerance: rel-L2 <= 1e-5 and max-abs <= 1e-5 * max|reference output|; the
@@ -177,12 +178,22 @@ def test_subsampled_matches_reference_product(refgpu, orc, shape, kshape):
     """convolution3DfftCUDAInPlaceSaveMemory against the reference's own
     subsampled-kernel product (modulateAndNormalizeSubsampled_kernel,
     src/convolution3Dfft.cu:65-125) driven on cuFFT by oracle/ref_subsampled.cu,
-    and both against the FP64 restatement.  Image extents are powers of two, so
-    the ratio k/n is exact in float32 under the reference's fast-math division
-    and the nearest-coefficient indices agree; kernel x extents are even, where
-    the reference reads inside its half-spectrum rows (for odd ones it reads one
+    and against the FP64 restatement.  Image extents are powers of two, so the
+    ratio k/n is exact in float32 under the reference's fast-math division and
+    the nearest-coefficient indices agree; kernel x extents are even, where the
+    reference reads inside its half-spectrum rows (for odd ones it reads one
     coefficient past a row at the x Nyquist, where this library takes the
-    Hermitian mirror)."""
+    Hermitian mirror).
+
+    The nearest-coefficient product is not Hermitian on the x DC and Nyquist
+    planes (index ties round up on both sides of zero), and what an inverse
+    real transform does with the imaginary parts there is left to the
+    implementation: this library drops them after the z and y inverses, as
+    numpy's irfftn does; cuFFT's C2R agrees at x = 512 and differs at x = 128
+    and 256.  Any treatment of those two bins changes the output only by a
+    term of period 2 along x, so the reference's output is compared on every
+    other x frequency (its spectrum at 0 < fx < nx/2), and the whole output
+    against the FP64 restatement."""
     rng = np.random.Generator(np.random.PCG64(sum(shape)))
     im = rng.random(shape).astype(np.float32)
     k = _gauss(kshape, (kshape[0] / 6, kshape[1] / 6, kshape[2] / 6))
@@ -193,8 +204,16 @@ def test_subsampled_matches_reference_product(refgpu, orc, shape, kshape):
     fc.convolution3DfftCUDAInPlaceSaveMemory(ours, (nx, ny, nz), k, (kx, ky, kz), 0)
     exact = orc.subsampled_fp64(im, k)
     rr, rm = _cmp(ref, exact)
-    print(f"{shape} {kshape}: reference product vs FP64 restatement rel-L2 {rr:.3e} max {rm:.3e}")
-    _check(ours, ref, f"{shape} {kshape} ours vs reference subsampled product")
+    print(f"{shape} {kshape}: reference product vs FP64 restatement, whole output: rel-L2 {rr:.3e} max {rm:.3e}")
+    band = (slice(None), slice(None), slice(1, nx // 2))
+    fr = np.fft.rfftn(ref.astype(np.float64))[band]
+    fo = np.fft.rfftn(ours.astype(np.float64))[band]
+    fe = np.fft.rfftn(exact)[band]
+    rb = float(np.linalg.norm(fo - fr) / np.linalg.norm(fr))
+    re_ = float(np.linalg.norm(fr - fe) / np.linalg.norm(fe))
+    print(f"{shape} {kshape}: x frequencies 0 < fx < nx/2: ours vs reference rel-L2 {rb:.3e}, "
+          f"reference vs FP64 {re_:.3e}")
+    assert rb <= REL_TOL, f"ours vs reference product off the x DC/Nyquist planes: rel-L2 {rb:.3e}"
     _check(ours, exact, f"{shape} {kshape} ours vs FP64 restatement")
 
 
