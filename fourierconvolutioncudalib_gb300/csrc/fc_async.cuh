@@ -52,6 +52,21 @@ __device__ __forceinline__ void tensor_load_3d(void* dst, const void* tmap, int 
       : "memory");
 }
 
+// shared -> global tile copy through a tensor map (TMA store, bulk-group
+// completion): the box at non-negative element coordinates (x, y, z); the
+// parts of the box outside the map's extents are not written.  src 128-byte
+// aligned and written before a proxy_fence() and a barrier.
+__device__ __forceinline__ void tensor_store_3d(const void* tmap, int x, int y, int z, const void* src) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(tmap),
+               "r"(x), "r"(y), "r"(z), "r"(smem_addr(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the bulk groups this thread committed have read their shared-memory sources
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// ... and their writes are complete
+__device__ __forceinline__ void bulk_wait() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 __device__ __forceinline__ bool bar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(

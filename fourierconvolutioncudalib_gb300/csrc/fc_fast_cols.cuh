@@ -110,6 +110,13 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* d
 // radix chain sit in shared memory.  Every box starts 128-byte aligned
 // (lengths that fail it keep k_cols); waits are bounded as in the fused z
 // pass.
+// tiles written back by tensor-map stores staged in shared memory (bit 0: the
+// persistent y pass, bit 1: the persistent fused z pass) instead of per-thread
+// global stores; 0 for comparison builds
+#ifndef FC_STORE_TMA
+#define FC_STORE_TMA 3
+#endif
+
 template <int N>
 struct YPipe {
   using G = ColGeom<N>;
@@ -139,6 +146,10 @@ __global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restr
   using P = YPipe<N>;
   constexpr int B = P::B;
   constexpr int R0 = first_radix<N, false>(), RF = last_radix<N, false>();
+  // rows of 64 bytes or more: the tensor store measured faster than the
+  // per-thread stores for 512-long columns (8-column tiles) and slower for
+  // 1024-long ones (4-column tiles, 32-byte rows)
+  constexpr bool kStore = (FC_STORE_TMA & 1) != 0 && B * (int)sizeof(float2) >= 64;
   extern __shared__ __align__(128) unsigned char ypsm[];
   float2* xch = reinterpret_cast<float2*>(ypsm);
   float2* ist = reinterpret_cast<float2*>(ypsm + P::ISTAGE_OFF);
@@ -188,13 +199,32 @@ __global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restr
       v[q] = (ok && j >= 0) ? ist[j * B + c] : make_float2(0.f, 0.f);
     }
     async::proxy_fence();
-    __syncthreads();  // every thread has read ISTAGE
+    if (kStore && tid == 0) async::bulk_wait_read();  // the previous tile's store has read XCH
+    __syncthreads();  // every thread has read ISTAGE (and XCH is free)
     if (ti + (int)gridDim.x < ntiles) {
       if (tid == 0) issue(ti + (int)gridDim.x);
       pend = true;
     }
     fft<N, INV, tc::kNone, false, true>(v, lay, t, tws);
-    if (ok) {
+    if constexpr (kStore) {
+      // the tile as rows of B columns in XCH (the transform's last exchange
+      // has been read), then one tensor store per box; the store leaves out
+      // the columns past ncols
+#pragma unroll
+      for (int q = 0; q < kVals; ++q) {
+        const int j = stage_pos<N, RF>(t, q);
+        if (j >= 0) xch[j * B + c] = v[q];
+      }
+      async::proxy_fence();
+      __syncthreads();
+      if (tid == 0) {
+        const int bx = ti % ntx;
+#pragma unroll
+        for (int b = 0; b < P::NBOX; ++b)
+          async::tensor_store_3d(&map, bx * B, b * P::YBOX, plane, xch + b * P::YBOX * B);
+        async::bulk_commit();
+      }
+    } else if (ok) {
       float2* d = S + (long long)plane * ps + col;
 #pragma unroll
       for (int q = 0; q < kVals; ++q) {
@@ -207,6 +237,7 @@ __global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restr
     if (tid == 0) atomicAdd(&g_ypipe_timeouts, 1u);
     if (pend) (void)async::bar_wait(bar, ph);
   }
+  if (kStore && tid == 0) async::bulk_wait();  // the tile stores are complete before the CTA ends
 }
 
 // Host: encode a 3-D tensor map of a spectrum of ncols columns (row pitch
@@ -467,6 +498,7 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
   using P = ZPipe<N>;
   constexpr int B = P::B;
   constexpr int R0 = first_radix<N, kZRev>(), RF = last_radix<N, !kZRev>();
+  constexpr bool kStore = (FC_STORE_TMA & 2) != 0;
   extern __shared__ __align__(128) unsigned char zpsm[];
   float2* xch = reinterpret_cast<float2*>(zpsm);
   float2* ist = reinterpret_cast<float2*>(zpsm + P::ISTAGE_OFF);
@@ -524,6 +556,7 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
     const long long next = ti + gridDim.x;
     float2 v[kVals];
     // ---- kernel column: load from KSTAGE, forward transform, park in KSTAGE
+    if (kStore && tid == 0) async::bulk_wait_read();  // the previous tile's store has read XCH
     if (!__syncthreads_and(async::bar_wait(kbar, ph))) {
       expired = true;
       break;
@@ -572,7 +605,26 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
       kpend = true;
     }
     fft<N, true, tc::kNone, !kZRev, true>(v, lay, t, twi);
-    if (ok) {
+    if constexpr (kStore) {
+      // the tile as rows of B columns in XCH (the inverse's last exchange has
+      // been read), then one tensor store per box; the store leaves out the
+      // columns past ncols.  The next tile's first exchange waits for the
+      // store to have read XCH (the wait before its first barrier).
+#pragma unroll
+      for (int q = 0; q < kVals; ++q) {
+        const int z = stage_pos<N, RF>(t, q);
+        if (z >= 0) xch[z * B + c] = v[q];
+      }
+      async::proxy_fence();
+      __syncthreads();
+      if (tid == 0) {
+        const int bx = (int)(ti % ntx);
+#pragma unroll
+        for (int b = 0; b < P::NBOX; ++b)
+          async::tensor_store_3d(&imap, bx * B, ky, b * P::ZBOX, xch + b * P::ZBOX * B);
+        async::bulk_commit();
+      }
+    } else if (ok) {
       float2* base = S + (long long)ky * pitch + col;
 #pragma unroll
       for (int q = 0; q < kVals; ++q) {
@@ -588,6 +640,7 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
     if (kpend) (void)async::bar_wait(kbar, ph);
     if (ipend) (void)async::bar_wait(ibar, ph);
   }
+  if (kStore && tid == 0) async::bulk_wait();  // the tile stores are complete before the CTA ends
 }
 
 // Host: encode the tensor map of k_zconv's image stage for a spectrum of ncols
