@@ -293,8 +293,11 @@ static cudaError_t cols_pipe_launch(float2* S, long long ps, long long es, int n
 //
 // The single-volume kernel uses tiles of at most 16 columns: the spectrum has
 // nx/2+1 columns, and narrower tiles waste less work on the ragged last tile.
+#ifndef FC_ZTILE256_B
+#define FC_ZTILE256_B 16
+#endif
 template <int N>
-using ZTile = ColGeomB<N, 16>;
+using ZTile = ColGeomB<N, N == 256 ? FC_ZTILE256_B : 16>;
 // radix order of the fused z pass: its forward transforms run the reversed
 // chain and its inverse the forward chain (either pairing hands the spectrum
 // over in registers; this one measured 0.4-2 % faster on GB300)
