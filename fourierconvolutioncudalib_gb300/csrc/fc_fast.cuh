@@ -121,12 +121,17 @@ __device__ __forceinline__ int rpad(int i) { return i + (i >> 4); }
 // conflicts.  A run i0 + m*step (m = 0, 1, ...) is at at(i0) + run_off(m, step)
 // whenever no run crosses pad boundaries differently from its first element
 // (lin_write / lin_read below), so its addresses fold into constant offsets.
-struct RowLay {
+// one line of a row tile; WS: the line's threads sit in one warp (T divides
+// 32), so its exchanges synchronise the warp instead of the CTA
+template <bool WS = false>
+struct RowLayT {
   float2* base;
   static constexpr int E = 1, D = 16;
+  static constexpr bool kWarpSync = WS;
   __device__ __forceinline__ float2* at(int i) const { return base + rpad(i); }
   __device__ __forceinline__ float2& operator[](int i) const { return base[rpad(i)]; }
 };
+using RowLay = RowLayT<false>;
 // column tile: B adjacent columns, position i of column c
 template <int B>
 struct ColLay {
@@ -134,6 +139,7 @@ struct ColLay {
   int c;
   static constexpr int E = B >= 16 ? B + B / 16 : B;
   static constexpr int D = B >= 16 ? 0 : 16 / B;
+  static constexpr bool kWarpSync = false;
   __device__ __forceinline__ float2* at(int i) const {
     const int q = i * B;
     return base + q + c + (q >> 4);
@@ -196,7 +202,9 @@ __device__ __forceinline__ void stage(float2 (&v)[kVals], const int t, const flo
   (void)tcx;
 }
 
-template <int N, int R, int NS, int R2, class L>
+// TAIL: end with the barrier that lets the exchange area be written again;
+// false where the caller passes a CTA barrier before its next write there
+template <int N, int R, int NS, int R2, bool TAIL = true, class L>
 __device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const int t) {
   constexpr int U = kVals / R, A = Plan<N>::A(R), NB = N / R;
   constexpr int U2 = kVals / R2, A2 = Plan<N>::A(R2), NB2 = N / R2;
@@ -216,7 +224,10 @@ __device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const 
       }
     }
   }
-  __syncthreads();
+  if constexpr (L::kWarpSync)
+    __syncwarp();
+  else
+    __syncthreads();
 #pragma unroll
   for (int b = 0; b < U2; ++b) {
     const int j = t + b * A2;
@@ -231,11 +242,18 @@ __device__ __forceinline__ void exchange(float2 (&v)[kVals], const L& sm, const 
       }
     }
   }
-  __syncthreads();
+  if constexpr (TAIL) {
+    if constexpr (L::kWarpSync)
+      __syncwarp();
+    else
+      __syncthreads();
+  }
 }
 
-// stages I .. S-1 of the forward chain (INV = false) or of the reversed chain (INV = true)
-template <int N, int I, int NS, bool INV, int TCM, bool REV = INV, bool TWS = false>
+// stages I .. S-1 of the forward chain (INV = false) or of the reversed chain (INV = true).
+// LASTSYNC false: the last exchange leaves out its closing barrier (the caller
+// passes a CTA barrier before it next writes the exchange area).
+template <int N, int I, int NS, bool INV, int TCM, bool REV = INV, bool TWS = false, bool LASTSYNC = true>
 struct Chain {
   template <class L>
   static __device__ __forceinline__ void run(float2 (&v)[kVals], const L& sm, const int t,
@@ -244,8 +262,8 @@ struct Chain {
     stage<N, I, R, NS, INV, TCM, REV, TWS>(v, t, W, tcx);
     if constexpr (I + 1 < Plan<N>::S) {
       constexpr int R2 = Plan<N>::radix(I + 1, REV);
-      exchange<N, R, NS, R2>(v, sm, t);
-      Chain<N, I + 1, NS * R, INV, TCM, REV, TWS>::run(v, sm, t, W, tcx);
+      exchange<N, R, NS, R2, (LASTSYNC || I + 2 < Plan<N>::S)>(v, sm, t);
+      Chain<N, I + 1, NS * R, INV, TCM, REV, TWS, LASTSYNC>::run(v, sm, t, W, tcx);
     }
   }
 };
@@ -254,11 +272,11 @@ struct Chain {
 // the tensor-core 16-point DFT for the radix-16 stages (tc::kFp16 / kBf16).
 // REV: radix order (false: the forward chain, true: the reversed chain).  A
 // transform that consumes another's outputs in registers runs the other's
-// order reversed; a standalone pass may run either.
-template <int N, bool INV, int TCM = tc::kNone, bool REV = INV, bool TWS = false, class L>
+// order reversed; a standalone pass may run either.  LASTSYNC as in Chain.
+template <int N, bool INV, int TCM = tc::kNone, bool REV = INV, bool TWS = false, bool LASTSYNC = true, class L>
 __device__ __forceinline__ void fft(float2 (&v)[kVals], const L& sm, const int t, const float2* __restrict__ W,
                                     const TcCtx& tcx = TcCtx{nullptr}) {
-  Chain<N, 0, 1, INV, TCM, REV, TWS>::run(v, sm, t, W, tcx);
+  Chain<N, 0, 1, INV, TCM, REV, TWS, LASTSYNC>::run(v, sm, t, W, tcx);
 }
 
 // Stage tables of one chain: Plan<N>::tab_size(REV) entries starting at the

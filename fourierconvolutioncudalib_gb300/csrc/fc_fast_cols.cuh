@@ -116,6 +116,15 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* d
 #ifndef FC_STORE_TMA
 #define FC_STORE_TMA 3
 #endif
+// the persistent fused z pass leaves out a transform's closing barrier where a
+// CTA barrier follows before the exchange area is written again (0 for comparison builds)
+#ifndef FC_TAIL_SKIP
+#define FC_TAIL_SKIP 1
+#endif
+// the fused z pass issues the next image copy together with the next kernel copy (0 for comparison builds)
+#ifndef FC_ZIMG_LATE
+#define FC_ZIMG_LATE 1
+#endif
 
 template <int N>
 struct YPipe {
@@ -205,6 +214,9 @@ __global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restr
       if (tid == 0) issue(ti + (int)gridDim.x);
       pend = true;
     }
+    // the closing barrier stays: the staged stores write the exchange area
+    // next, and without it the per-thread stores of 1024-long columns
+    // measured 8-13 % slower (1024x1024x256)
     fft<N, INV, tc::kNone, false, true>(v, lay, t, tws);
     if constexpr (kStore) {
       // the tile as rows of B columns in XCH (the transform's last exchange
@@ -293,11 +305,8 @@ static cudaError_t cols_pipe_launch(float2* S, long long ps, long long es, int n
 //
 // The single-volume kernel uses tiles of at most 16 columns: the spectrum has
 // nx/2+1 columns, and narrower tiles waste less work on the ragged last tile.
-#ifndef FC_ZTILE256_B
-#define FC_ZTILE256_B 16
-#endif
 template <int N>
-using ZTile = ColGeomB<N, N == 256 ? FC_ZTILE256_B : 16>;
+using ZTile = ColGeomB<N, 16>;
 // radix order of the fused z pass: its forward transforms run the reversed
 // chain and its inverse the forward chain (either pairing hands the spectrum
 // over in registers; this one measured 0.4-2 % faster on GB300)
@@ -502,6 +511,9 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
   constexpr int B = P::B;
   constexpr int R0 = first_radix<N, kZRev>(), RF = last_radix<N, !kZRev>();
   constexpr bool kStore = (FC_STORE_TMA & 2) != 0;
+  // the next tile's image copy is issued with its kernel copy, after the
+  // product's barrier, instead of after a barrier of its own
+  constexpr bool kLateImage = FC_ZIMG_LATE != 0;
   extern __shared__ __align__(128) unsigned char zpsm[];
   float2* xch = reinterpret_cast<float2*>(zpsm);
   float2* ist = reinterpret_cast<float2*>(zpsm + P::ISTAGE_OFF);
@@ -573,7 +585,8 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
       v[q] = (ok && z >= 0 && p < kplanes) ? kst[p * B + c] : make_float2(0.f, 0.f);
     }
     if constexpr (Plan<N>::S == 1) __syncthreads();  // no exchange barrier inside the transform
-    fft<N, false, tc::kNone, kZRev, true>(v, lay, t, twf);
+    // (the image wait below is the CTA barrier before the exchange area is next written)
+    fft<N, false, tc::kNone, kZRev, true, !FC_TAIL_SKIP>(v, lay, t, twf);
 #pragma unroll
     for (int q = 0; q < kVals; ++q) kst[q * P::THREADS + tid] = v[q];
     // ---- image tile: load from ISTAGE, then the next tile's image copy
@@ -587,13 +600,16 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
       const int z = stage_pos<N, R0>(t, q);
       v[q] = (ok && z >= 0) ? ist[z * B + c] : make_float2(0.f, 0.f);
     }
-    async::proxy_fence();
-    __syncthreads();  // every thread has read ISTAGE
-    if (next < ntiles) {
-      if (tid == 0) issue_image(next);
-      ipend = true;
+    if constexpr (!kLateImage) {
+      async::proxy_fence();
+      __syncthreads();  // every thread has read ISTAGE
+      if (next < ntiles) {
+        if (tid == 0) issue_image(next);
+        ipend = true;
+      }
     }
-    fft<N, false, tc::kNone, kZRev, true>(v, lay, t, twf);
+    // (the barrier after the product is the one before the next write of the exchange area)
+    fft<N, false, tc::kNone, kZRev, true, !FC_TAIL_SKIP>(v, lay, t, twf);
 #pragma unroll
     for (int q = 0; q < kVals; ++q) {
       float2 a = kst[q * P::THREADS + tid];  // kernel spectrum (d_Src of modulateAndNormalize_kernel)
@@ -602,12 +618,18 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
       v[q] = make_float2(scale * (a.x * b.x - a.y * b.y), scale * (a.y * b.x + a.x * b.y));
     }
     async::proxy_fence();
-    __syncthreads();  // every thread has read its parked kernel spectrum
+    __syncthreads();  // every thread has read its parked kernel spectrum (and ISTAGE)
     if (next < ntiles) {
-      if (tid == 0) issue_kernel(next);
+      if (tid == 0) {
+        issue_kernel(next);
+        if (kLateImage) issue_image(next);
+      }
       kpend = true;
+      if (kLateImage) ipend = true;
     }
-    fft<N, true, tc::kNone, !kZRev, true>(v, lay, t, twi);
+    // staged stores write the exchange area next: keep the closing barrier;
+    // per-thread stores reach the next tile's first barrier before it
+    fft<N, true, tc::kNone, !kZRev, true, kStore || !FC_TAIL_SKIP>(v, lay, t, twi);
     if constexpr (kStore) {
       // the tile as rows of B columns in XCH (the inverse's last exchange has
       // been read), then one tensor store per box; the store leaves out the

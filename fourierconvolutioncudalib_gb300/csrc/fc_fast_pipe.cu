@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
   const int tid = (int)threadIdx.x;
   const long long ntiles = RowGeom<N>::tiles(nrows);
   const long long row_bytes = in_pitch * (C2R ? (long long)sizeof(float2) : (long long)sizeof(float));
+  const bool skip = async::copies_skipped();  // read once: a global load per tile would delay warp 0
   async::pdl_launch_dependents();
   if (tid == 0) {
     async::bar_init(&bar, 1);
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
     const long long nr = (nrows - r0) < P::ROWS ? (nrows - r0) : P::ROWS;
     const uint32_t bytes = (uint32_t)(nr * row_bytes);
     async::bar_expect(&bar, bytes);
-    if (!async::copies_skipped()) async::bulk_load(buf, in + r0 * row_bytes, bytes, &bar);
+    if (!skip) async::bulk_load(buf, in + r0 * row_bytes, bytes, &bar);
   };
   if (tid == 0 && tile < ntiles) issue(tile);
   uint32_t phase = 0;

@@ -28,6 +28,16 @@ struct RowGeom {
   __host__ __device__ static long long tiles(long long nrows) { return (nrows + 2LL * LPB - 1) / (2LL * LPB); }
 };
 
+// a line's T threads lie in one warp when T divides 32 (lines start at
+// multiples of T); its exchanges then synchronise that warp only.  The
+// tensor-core transforms keep CTA barriers.  FC_ROW_WARPSYNC=0 builds the CTA
+// barriers everywhere, for comparison builds.
+#ifndef FC_ROW_WARPSYNC
+#define FC_ROW_WARPSYNC 1
+#endif
+template <int N, int TCM>
+constexpr bool kLineWarp = FC_ROW_WARPSYNC && TCM == tc::kNone && 32 % RowGeom<N>::T == 0;
+
 // line / thread split of a row tile: tile rows ra = 2*(tile*LPB + line), rb = ra + 1
 template <int N>
 struct RowSlot {
@@ -66,25 +76,30 @@ __device__ __forceinline__ void finish_r2c(float2 (&v)[kVals], const RowSlot<N>&
   using G = RowGeom<N>;
   constexpr int RF = last_radix<N, REV>();
   constexpr int NBF = N / RF, UF = kVals / RF, AF = Plan<N>::A(RF);
+  constexpr bool WS = kLineWarp<N, TCM>;
+  using Lay = RowLayT<WS>;
   float2* lbase = sm + s.line * G::LS;
-  const RowLay lay{lbase};
+  const Lay lay{lbase};
   fft<N, false, TCM, REV, TWS>(v, lay, s.t, W, tcx);
   // natural-order outputs x = j + m*NBF of the last stage into the line
 #pragma unroll
   for (int b = 0; b < UF; ++b) {
     const int j = s.t + b * AF;
     if (j < NBF && s.t < AF) {
-      if constexpr (lin_read<RowLay>(NBF)) {
+      if constexpr (lin_read<Lay>(NBF)) {
         float2* p = lay.at(j);
 #pragma unroll
-        for (int m = 0; m < RF; ++m) p[run_off<RowLay>(m, NBF)] = v[b * RF + m];
+        for (int m = 0; m < RF; ++m) p[run_off<Lay>(m, NBF)] = v[b * RF + m];
       } else {
 #pragma unroll
         for (int m = 0; m < RF; ++m) lay[j + m * NBF] = v[b * RF + m];
       }
     }
   }
-  __syncthreads();
+  if constexpr (WS)
+    __syncwarp();
+  else
+    __syncthreads();
   if (s.act) {
     for (int k = s.t; k <= N / 2; k += G::T) {
       const float2 zk = lbase[rpad(k)];
@@ -141,7 +156,7 @@ __device__ __forceinline__ void finish_c2r(float2 (&v)[kVals], const RowSlot<N>&
                                            const TcCtx& tcx = TcCtx{nullptr}) {
   using G = RowGeom<N>;
   constexpr int RF = last_radix<N, REV>();
-  fft<N, true, TCM, REV, TWS>(v, RowLay{sm + s.line * G::LS}, s.t, W, tcx);
+  fft<N, true, TCM, REV, TWS>(v, RowLayT<kLineWarp<N, TCM>>{sm + s.line * G::LS}, s.t, W, tcx);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int x = stage_pos<N, RF>(s.t, q);
