@@ -57,6 +57,8 @@ CONFIGS = {
     "c2b": dict(workload="plain_conv_384x448x96_psf31x31x63", fn="c2", kw=dict(nonpow2=True)),
     "c1": dict(workload="plain_conv_64x64x64_psf7x7x7", fn="c1", kw={}),
     "c5": dict(workload="plain_conv_1024x1024x256_psf63x63x63", fn="c5", kw={}),
+    # the 256-long fused z pass on a quarter of the columns (profiler captures)
+    "c5s": dict(workload="plain_conv_512x512x256_psf63x63x63", fn="c5", kw=dict(plane=512)),
 }
 METRIC = "Gvoxel/s per 3D FFT conv (plain/batched/adjoint/TC) vs plain & ref cuFFT, rel-L2<=1e-5"
 

@@ -113,9 +113,11 @@ def c4() -> List[Dict[str, np.ndarray]]:
     return views
 
 
-def c5() -> Dict[str, np.ndarray]:
+def c5(plane: int = 1024) -> Dict[str, np.ndarray]:
     """1024x1024x256 with 20000 spots (seed 6); 63^3 mixture of 3 anisotropic
-    Gaussians with weights 0.7 / 0.2 / 0.1, sum 1."""
-    im = spot_volume((256, 1024, 1024), 20000, 6)
+    Gaussians with weights 0.7 / 0.2 / 0.1, sum 1.  plane=512: the 512x512x256
+    case with 5000 spots and the same PSF (the same 256-long z pass on a
+    quarter of the columns, for profiler captures)."""
+    im = spot_volume((256, plane, plane), 20000 * (plane * plane) // (1024 * 1024), 6)
     mix = [(0.7, (3.0, 1.5, 1.5)), (0.2, (6.0, 3.0, 3.0)), (0.1, (10.0, 6.0, 6.0))]
     return dict(image=im, kernel=gaussian_psf((63, 63, 63), (1, 1, 1), mix=mix))
