@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restr
   const int ntx = (ncols + B - 1) / B;
   const int ntiles = ntx * nplanes;  // tile counts fit an int for every supported shape
   const bool skip = async::copies_skipped();
-  async::pdl_launch_dependents();
+  async::pdl_trigger_at_start<async::kPdlY>();
   auto issue = [&](int ti) {
     const int bx = ti % ntx, plane = ti / ntx;
     async::bar_expect(bar, (unsigned)P::IBYTES);
@@ -192,7 +192,9 @@ __global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restr
   bool expired = false;
   uint32_t ph = 0;
   const ColLay<B> lay{xch, c};
+  bool signalled = false;  // the successor may launch (programmatic dependent launch)
   for (; ti < ntiles; ti += (int)gridDim.x, ph ^= 1u) {
+    signalled |= async::pdl_trigger_last_tile<async::kPdlY>(ti + (int)gridDim.x >= ntiles);
     const int plane = ti / ntx;
     const int col = (ti % ntx) * B + c;
     const bool ok = col < ncols && t < P::G::T;
@@ -245,6 +247,7 @@ __global__ void __launch_bounds__(YPipe<N>::THREADS) k_cols_pipe(float2* __restr
       }
     }
   }
+  async::pdl_trigger_at_end<async::kPdlY>(signalled);
   if (expired) {
     if (tid == 0) atomicAdd(&g_ypipe_timeouts, 1u);
     if (pend) (void)async::bar_wait(bar, ph);
@@ -291,7 +294,8 @@ static cudaError_t cols_pipe_launch(float2* S, long long ps, long long es, int n
     const long long ntiles = (long long)((ncols + P::B - 1) / P::B) * nplanes;
     const long long grid = std::min<long long>(ntiles, (long long)occ * sms);
     *used = true;
-    return async::launch_pdl(kern, (unsigned)grid, P::THREADS, P::SMEM_BYTES, st, S, ps, es, ncols, nplanes, W, map);
+    return async::launch_pdl(async::kPdlY, kern, (unsigned)grid, P::THREADS, P::SMEM_BYTES, st, S, ps, es, ncols,
+                             nplanes, W, map);
   }
 }
 
@@ -530,7 +534,7 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
   const long long zs = (long long)ny * pitch;
   const unsigned kbytes = (unsigned)(nkbox * kbox * B * (int)sizeof(float2));
   const bool skip = async::copies_skipped();
-  async::pdl_launch_dependents();
+  async::pdl_trigger_at_start<async::kPdlZ>();
   auto issue_image = [&](long long ti) {
     const int bx = (int)(ti % ntx), ky = (int)(ti / ntx);
     async::bar_expect(ibar, (unsigned)P::IBYTES);
@@ -564,11 +568,13 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
   bool expired = false;
   uint32_t ph = 0;  // parity of the barriers' current phase (one phase per tile)
   const ColLay<B> lay{xch, c};
+  bool signalled = false;  // the successor may launch (programmatic dependent launch)
   for (; ti < ntiles; ti += gridDim.x, ph ^= 1u) {
     const int ky = (int)(ti / ntx);
     const int col = (int)(ti % ntx) * B + c;
     const bool ok = col < ncols && t < P::G::T;
     const long long next = ti + gridDim.x;
+    signalled |= async::pdl_trigger_last_tile<async::kPdlZ>(next >= ntiles);
     float2 v[kVals];
     // ---- kernel column: load from KSTAGE, forward transform, park in KSTAGE
     if (kStore && tid == 0) async::bulk_wait_read();  // the previous tile's store has read XCH
@@ -658,6 +664,7 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
       }
     }
   }
+  async::pdl_trigger_at_end<async::kPdlZ>(signalled);
   if (expired) {
     // a wait ran out: count it, then let the copies still in flight (both of
     // the current phase) land, with the same bounded wait, before returning
@@ -714,8 +721,8 @@ static cudaError_t zconv_pipe_launch(float2* S, const float2* KXY, long long pit
     const long long ntiles = (long long)((ncols + P::B - 1) / P::B) * ny;
     const long long grid = std::min<long long>(ntiles, (long long)occ * sms);
     *used = true;
-    return async::launch_pdl(kern, (unsigned)grid, P::THREADS, P::SMEM_BYTES, st, S, pitch, ny, ncols, kplanes, hz,
-                             scale, W, imap, kmap, kbox, nkb);
+    return async::launch_pdl(async::kPdlZ, kern, (unsigned)grid, P::THREADS, P::SMEM_BYTES, st, S, pitch, ny, ncols,
+                             kplanes, hz, scale, W, imap, kmap, kbox, nkb);
   }
 }
 // Host: enqueue a read of this translation unit's count of expired stage

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
   const long long ntiles = RowGeom<N>::tiles(nrows);
   const long long row_bytes = in_pitch * (C2R ? (long long)sizeof(float2) : (long long)sizeof(float));
   const bool skip = async::copies_skipped();  // read once: a global load per tile would delay warp 0
-  async::pdl_launch_dependents();
+  async::pdl_trigger_at_start<async::kPdlX>();
   if (tid == 0) {
     async::bar_init(&bar, 1);
     async::bar_init_fence();
@@ -65,7 +65,9 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
   };
   if (tid == 0 && tile < ntiles) issue(tile);
   uint32_t phase = 0;
+  bool signalled = false;  // the successor may launch (programmatic dependent launch)
   for (; tile < ntiles; tile += gridDim.x) {
+    signalled |= async::pdl_trigger_last_tile<async::kPdlX>(tile + gridDim.x >= ntiles);
     const bool ok = async::bar_wait(&bar, phase);
     if (!__syncthreads_and(ok)) {
       if (tid == 0) atomicAdd(&g_pipe_timeouts, 1u);
@@ -89,6 +91,7 @@ __global__ void __launch_bounds__(RowGeom<N>::THREADS, 3) k_rows_pipe(const char
     else
       finish_r2c<N>(v, s, reinterpret_cast<float2*>(out), out_pitch, W, sm);
   }
+  async::pdl_trigger_at_end<async::kPdlX>(signalled);
 }
 
 template <int N, bool C2R>
@@ -118,8 +121,8 @@ static cudaError_t run_rows_pipe(const void* in, long long in_pitch, void* out, 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long ntiles = G::tiles(nrows);
   const long long grid = std::min<long long>(ntiles, (long long)occ * sms);
-  return async::launch_pdl(kern, (unsigned)grid, G::THREADS, smem, st, reinterpret_cast<const char*>(in), in_pitch,
-                           out, out_pitch, nrows, W);
+  return async::launch_pdl(async::kPdlX, kern, (unsigned)grid, G::THREADS, smem, st, reinterpret_cast<const char*>(in),
+                           in_pitch, out, out_pitch, nrows, W);
 }
 
 }  // namespace fast
@@ -165,12 +168,13 @@ void pipe_timeouts_clear() {
 cudaError_t pipe_wait_ctl_set(long long limit, int skip_copies) { return async::wait_ctl_set_tu(limit, skip_copies); }
 
 namespace async {
-bool pdl_enabled() {
-  static const bool on = [] {
+bool pdl_enabled(int kind) {
+  // FC_PDL: a mask of kPdlX | kPdlY | kPdlZ (0: none); default FC_PDL_DEFAULT
+  static const int mask = [] {
     const char* e = std::getenv("FC_PDL");
-    return !e || std::atoi(e) != 0;
+    return e ? std::atoi(e) : FC_PDL_DEFAULT;
   }();
-  return on;
+  return (mask & kind) != 0;
 }
 }  // namespace async
 

@@ -5,9 +5,11 @@ asynchronous copies (x passes: bulk copies; fused z pass: tensor-map copies of
 the image tile and of the kernel planes; y passes, when selected: tensor-map
 copies) with programmatic dependent launch, or a one-tile-per-CTA kernel.  The
 selection is read from the environment once per process (FC_PIPE, FC_YPIPE,
-FC_ZPIPE, FC_PDL), so each variant runs in a child process.  Tolerance: rel-L2 <= 1e-5 and max-abs <= 1e-5 * max against the FP64
-oracle, on shapes that include columns longer than 256 (z = 300, 512, 1024:
-the tensor-map stage in two or four boxes).
+FC_ZPIPE, and FC_PDL, a mask of the pass kinds launched with programmatic
+dependent launch), so each variant runs in a child process.  Tolerance: rel-L2
+<= 1e-5 and max-abs <= 1e-5 * max against the FP64 oracle, on shapes that
+include columns longer than 256 (z = 300, 512, 1024: the tensor-map stage in
+two or four boxes).
 """
 import os
 import subprocess
@@ -44,9 +46,9 @@ print("ok")
 
 
 @pytest.mark.parametrize("env", [{}, {"FC_YPIPE": "1"}, {"FC_YPIPE": "0"}, {"FC_ZPIPE": "0"}, {"FC_PDL": "0"},
-                                 {"FC_PIPE": "0", "FC_PDL": "0", "FC_YPIPE": "1"}],
+                                 {"FC_PDL": "5"}, {"FC_PIPE": "0", "FC_PDL": "0", "FC_YPIPE": "1"}],
                          ids=["default", "y-tensor-map-all", "y-one-tile-per-cta", "z-one-tile-per-cta", "no-pdl",
-                              "x-one-tile-per-cta"])
+                              "pdl-x-and-z-only", "x-one-tile-per-cta"])
 def test_pass_kernel_variants(cuda, fclib, env):
     e = dict(os.environ)
     e.update(env)
