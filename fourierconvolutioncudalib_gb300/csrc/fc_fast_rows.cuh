@@ -37,6 +37,14 @@ struct RowGeom {
 #endif
 template <int N, int TCM>
 constexpr bool kLineWarp = FC_ROW_WARPSYNC && TCM == tc::kNone && 32 % RowGeom<N>::T == 0;
+// the R2C pairs Z[k] with Z[N-k] by warp shuffles: a line of 32 threads (one
+// warp) whose last stage is radix 2 over 32 butterfly columns (N = 512);
+// FC_ROW_SHFL=0 builds the shared-memory pairing, for comparison builds
+#ifndef FC_ROW_SHFL
+#define FC_ROW_SHFL 1
+#endif
+template <int N, int RF, int AF, bool WS>
+constexpr bool kShflPair = FC_ROW_SHFL && WS && RowGeom<N>::T == 32 && RF == 2 && AF == 32 && N == 64 * (kVals / 2);
 
 // line / thread split of a row tile: tile rows ra = 2*(tile*LPB + line), rb = ra + 1
 template <int N>
@@ -81,6 +89,31 @@ __device__ __forceinline__ void finish_r2c(float2 (&v)[kVals], const RowSlot<N>&
   float2* lbase = sm + s.line * G::LS;
   const Lay lay{lbase};
   fft<N, false, TCM, REV, TWS>(v, lay, s.t, W, tcx);
+  if constexpr (kShflPair<N, RF, AF, WS>) {
+    // The line is one warp and lane t holds Z[k] for k = t + 32 b + (N/2) m in
+    // v[2b + m]; Z[N - k] sits in lane (32 - t) mod 32, in v[2(UF-1-b) + 1-m]
+    // for t != 0 and in v[2(UF-b) + 1-m] for t == 0 (v[m] itself for k = 0,
+    // N/2).  Each lane offers the register its partner lane asks for, so one
+    // shuffle per value pairs the spectra without a trip through shared memory.
+    const int lane = (int)(threadIdx.x & 31u);
+    const int from = (32 - lane) & 31;
+#pragma unroll
+    for (int b = 0; b < UF; ++b) {
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        if (m == 1 && b != 0) continue;  // k > N/2: not stored
+        const float2 mine = lane == 0 ? v[b == 0 ? m : 2 * (UF - b) + 1 - m] : v[2 * (UF - 1 - b) + 1 - m];
+        const float2 zn = make_float2(__shfl_sync(0xffffffffu, mine.x, from), __shfl_sync(0xffffffffu, mine.y, from));
+        const float2 zk = v[2 * b + m];
+        const int k = lane + 32 * b + (N / 2) * m;
+        if (s.act && (m == 0 || lane == 0)) {
+          if (s.va) out[s.ra * out_pitch + k] = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+          if (s.vb) out[s.rb * out_pitch + k] = make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x));
+        }
+      }
+    }
+    return;
+  }
   // natural-order outputs x = j + m*NBF of the last stage into the line
 #pragma unroll
   for (int b = 0; b < UF; ++b) {
