@@ -125,6 +125,10 @@ __global__ void __launch_bounds__(ColGeom<N>::THREADS) k_cols(Src src, float2* d
 #ifndef FC_ZIMG_LATE
 #define FC_ZIMG_LATE 1
 #endif
+// the fused z pass takes the last spectrum column in 8-row tiles (0 for comparison builds)
+#ifndef FC_ZNYQ
+#define FC_ZNYQ 1
+#endif
 
 template <int N>
 struct YPipe {
@@ -510,7 +514,8 @@ template <int N, bool CONJ>
 __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
     k_zconv_pipe(float2* __restrict__ S, long long pitch, int ny, int ncols, int kplanes, int hz, float scale,
                  const float2* __restrict__ W, const __grid_constant__ CUtensorMap imap,
-                 const __grid_constant__ CUtensorMap kmap, int kbox, int nkbox) {
+                 const __grid_constant__ CUtensorMap kmap, int kbox, int nkbox,
+                 const __grid_constant__ CUtensorMap nimap, const __grid_constant__ CUtensorMap nkmap, int nyq_tiles) {
   using P = ZPipe<N>;
   constexpr int B = P::B;
   constexpr int R0 = first_radix<N, kZRev>(), RF = last_radix<N, !kZRev>();
@@ -529,25 +534,45 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
   const int tid = (int)threadIdx.x;
   const int c = tid % B;
   const int t = tid / B;
-  const int ntx = (ncols + B - 1) / B;
-  const long long ntiles = (long long)ntx * ny;
+  // nyq_tiles > 0: the last column of the spectrum (ncols = 16 k + 1 or + 2)
+  // goes in tiles of 8 rows x 2 columns (boxes of nimap / nkmap, laid out as a
+  // 16-column tile: column c of the tile is row c / 2, column c % 2 of the
+  // box; the second column is past the spectrum: zeros in, not stored),
+  // after the full 16-column tiles, instead of one tile of 1 column per row
+  const int ntx = nyq_tiles > 0 ? ncols / B : (ncols + B - 1) / B;
+  const long long nmain = (long long)ntx * ny;
+  const long long ntiles = nmain + nyq_tiles;
+  const int nyq_col = ntx * B;
   const long long zs = (long long)ny * pitch;
   const unsigned kbytes = (unsigned)(nkbox * kbox * B * (int)sizeof(float2));
   const bool skip = async::copies_skipped();
   async::pdl_trigger_at_start<async::kPdlZ>();
   auto issue_image = [&](long long ti) {
-    const int bx = (int)(ti % ntx), ky = (int)(ti / ntx);
     async::bar_expect(ibar, (unsigned)P::IBYTES);
-    if (!skip)
+    if (skip) return;
+    if (ti < nmain) {
+      const int bx = (int)(ti % ntx), ky = (int)(ti / ntx);
 #pragma unroll
       for (int b = 0; b < P::NBOX; ++b)
         async::tensor_load_3d(ist + b * P::ZBOX * B, &imap, bx * B, ky, b * P::ZBOX, ibar);
+    } else {
+      const int ky0 = (int)(ti - nmain) * (B / 2);
+#pragma unroll
+      for (int b = 0; b < P::NBOX; ++b)
+        async::tensor_load_3d(ist + b * P::ZBOX * B, &nimap, nyq_col, ky0, b * P::ZBOX, ibar);
+    }
   };
   auto issue_kernel = [&](long long ti) {
-    const int bx = (int)(ti % ntx), ky = (int)(ti / ntx);
     async::bar_expect(kbar, kbytes);
-    if (!skip)
+    if (skip) return;
+    if (ti < nmain) {
+      const int bx = (int)(ti % ntx), ky = (int)(ti / ntx);
       for (int b = 0; b < nkbox; ++b) async::tensor_load_3d(kst + b * kbox * B, &kmap, bx * B, ky, b * kbox, kbar);
+    } else {
+      const int ky0 = (int)(ti - nmain) * (B / 2);
+      for (int b = 0; b < nkbox; ++b)
+        async::tensor_load_3d(kst + b * kbox * B, &nkmap, nyq_col, ky0, b * kbox, kbar);
+    }
   };
   // the twiddle tables are not written by any pass
   copy_stage_tables<N, kZRev>(twf, W, tid, P::THREADS);
@@ -570,9 +595,10 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
   const ColLay<B> lay{xch, c};
   bool signalled = false;  // the successor may launch (programmatic dependent launch)
   for (; ti < ntiles; ti += gridDim.x, ph ^= 1u) {
-    const int ky = (int)(ti / ntx);
-    const int col = (int)(ti % ntx) * B + c;
-    const bool ok = col < ncols && t < P::G::T;
+    const bool nyq = ti >= nmain;
+    const int ky = nyq ? 0 : (int)(ti / ntx);
+    const int col = nyq ? 0 : (int)(ti % ntx) * B + c;
+    const bool ok = (nyq || col < ncols) && t < P::G::T;
     const long long next = ti + gridDim.x;
     signalled |= async::pdl_trigger_last_tile<async::kPdlZ>(next >= ntiles);
     float2 v[kVals];
@@ -649,10 +675,17 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
       async::proxy_fence();
       __syncthreads();
       if (tid == 0) {
-        const int bx = (int)(ti % ntx);
+        if (!nyq) {
+          const int bx = (int)(ti % ntx);
 #pragma unroll
-        for (int b = 0; b < P::NBOX; ++b)
-          async::tensor_store_3d(&imap, bx * B, ky, b * P::ZBOX, xch + b * P::ZBOX * B);
+          for (int b = 0; b < P::NBOX; ++b)
+            async::tensor_store_3d(&imap, bx * B, ky, b * P::ZBOX, xch + b * P::ZBOX * B);
+        } else {
+          const int ky0 = (int)(ti - nmain) * (B / 2);
+#pragma unroll
+          for (int b = 0; b < P::NBOX; ++b)
+            async::tensor_store_3d(&nimap, nyq_col, ky0, b * P::ZBOX, xch + b * P::ZBOX * B);
+        }
         async::bulk_commit();
       }
     } else if (ok) {
@@ -700,10 +733,21 @@ static cudaError_t zconv_pipe_launch(float2* S, const float2* KXY, long long pit
     int kbox = (kplanes + nkb - 1) / nkb;
     kbox = (kbox + P::KROW_ALIGN - 1) / P::KROW_ALIGN * P::KROW_ALIGN;
     if (kbox > 256 || (long long)nkb * kbox * P::B > P::KCAP) return cudaSuccess;
-    CUtensorMap imap, kmap;
+    CUtensorMap imap, kmap, nimap, nkmap;
     if (!zstage_tensor_map(&imap, S, pitch, ny, ncols, N, P::B, P::ZBOX) ||
         !zstage_tensor_map(&kmap, KXY, pitch, ny, ncols, kplanes, P::B, kbox))
       return cudaSuccess;
+    // the last one or two columns in tiles of 8 rows x 2 columns (the fused
+    // pass writes its tiles back by tensor-map stores, which leave out what
+    // lies past the spectrum)
+    int nyq_tiles = 0;
+    const int rem = ncols % P::B;
+    if (FC_ZNYQ && (FC_STORE_TMA & 2) && P::B == 16 && (rem == 1 || rem == 2) && ncols > P::B &&
+        tile_tensor_map(&nimap, S, pitch, ny, ncols, N, 2, P::B / 2, P::ZBOX) &&
+        tile_tensor_map(&nkmap, KXY, pitch, ny, ncols, kplanes, 2, P::B / 2, kbox))
+      nyq_tiles = (ny + P::B / 2 - 1) / (P::B / 2);
+    else
+      nimap = imap, nkmap = kmap;
     auto kern = k_zconv_pipe<N, CONJ>;
     static int s_occ = 0;  // resident CTAs per SM of this instantiation (a benign race: same value)
     int occ = s_occ;
@@ -718,11 +762,12 @@ static cudaError_t zconv_pipe_launch(float2* S, const float2* KXY, long long pit
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long ntiles = (long long)((ncols + P::B - 1) / P::B) * ny;
+    const long long ntiles = nyq_tiles > 0 ? (long long)(ncols / P::B) * ny + nyq_tiles
+                                           : (long long)((ncols + P::B - 1) / P::B) * ny;
     const long long grid = std::min<long long>(ntiles, (long long)occ * sms);
     *used = true;
     return async::launch_pdl(async::kPdlZ, kern, (unsigned)grid, P::THREADS, P::SMEM_BYTES, st, S, pitch, ny, ncols,
-                             kplanes, hz, scale, W, imap, kmap, kbox, nkb);
+                             kplanes, hz, scale, W, imap, kmap, kbox, nkb, nimap, nkmap, nyq_tiles);
   }
 }
 // Host: enqueue a read of this translation unit's count of expired stage
