@@ -9,7 +9,8 @@ FC_ZPIPE, and FC_PDL, a mask of the pass kinds launched with programmatic
 dependent launch), so each variant runs in a child process.  Tolerance: rel-L2
 <= 1e-5 and max-abs <= 1e-5 * max against the FP64 oracle, on shapes that
 include columns longer than 256 (z = 300, 512, 1024: the tensor-map stage in
-two or four boxes).
+two or four boxes) and spectra whose last one or two columns go in 8-row tiles
+with a partial last tile (x = 34 and 96 with y = 36 and 44).
 """
 import os
 import subprocess
@@ -31,7 +32,8 @@ from oracle import oracle as orc
 fc.load_library()
 rng = np.random.default_rng(5)
 for shape, kshape in (((128, 512, 512), (63, 31, 31)), ((96, 448, 384), (31, 15, 21)), ((200, 96, 224), (7, 5, 9)),
-                      ((300, 64, 64), (9, 9, 9)), ((512, 32, 48), (15, 5, 7)), ((1024, 16, 32), (21, 3, 3))):
+                      ((300, 64, 64), (9, 9, 9)), ((512, 32, 48), (15, 5, 7)), ((1024, 16, 32), (21, 3, 3)),
+                      ((64, 36, 34), (9, 5, 5)), ((128, 44, 96), (15, 7, 9))):
     im = rng.random(shape, dtype=np.float32)
     k = rng.random(kshape, dtype=np.float32)
     k /= k.sum()
