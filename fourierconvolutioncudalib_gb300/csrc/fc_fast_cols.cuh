@@ -481,9 +481,14 @@ __global__ void __launch_bounds__(ZTile<N>::THREADS, ZGeom<N>::MIN_BLOCKS) k_zco
 // start 8000 bytes in) keep the one-tile-per-CTA kernel.  Waits are bounded:
 // a wait that runs out is counted, the CTA waits (bounded) for any copy it
 // still has in flight, and returns.
+// columns per tile of the persistent fused z pass (at most; 16 by default,
+// other widths for comparison builds)
+#ifndef FC_ZPIPE_B
+#define FC_ZPIPE_B 16
+#endif
 template <int N>
 struct ZPipe {
-  using G = ZTile<N>;
+  using G = ColGeomB<N, FC_ZPIPE_B>;
   static constexpr int B = G::B;
   static constexpr int THREADS = G::THREADS;
   static constexpr int XCH_BYTES = ((G::SMEM * (int)sizeof(float2) + 127) / 128) * 128;
@@ -507,7 +512,8 @@ struct ZPipe {
   static_assert((B * (int)sizeof(float2)) % 16 == 0, "box rows must be multiples of 16 bytes");
   static_assert(ISTAGE_OFF % 128 == 0 && KSTAGE_OFF % 128 == 0 && BAR_OFF % 128 == 0, "stage alignment");
   static constexpr bool OK = (ZBOX * B * (int)sizeof(float2)) % 128 == 0 && SMEM_BYTES <= 227 * 1024;
-  static constexpr int MIN_BLOCKS = ZGeom<N>::MIN_BLOCKS;
+  // resident CTAs asked of the register allocator: 512 threads per SM (at most 128 registers)
+  static constexpr int MIN_BLOCKS = THREADS <= 512 ? 512 / THREADS : 1;
 };
 
 template <int N, bool CONJ>
@@ -534,11 +540,11 @@ __global__ void __launch_bounds__(ZPipe<N>::THREADS, ZPipe<N>::MIN_BLOCKS)
   const int tid = (int)threadIdx.x;
   const int c = tid % B;
   const int t = tid / B;
-  // nyq_tiles > 0: the last column of the spectrum (ncols = 16 k + 1 or + 2)
-  // goes in tiles of 8 rows x 2 columns (boxes of nimap / nkmap, laid out as a
-  // 16-column tile: column c of the tile is row c / 2, column c % 2 of the
+  // nyq_tiles > 0: the last column of the spectrum (ncols = B k + 1 or + 2)
+  // goes in tiles of B/2 rows x 2 columns (boxes of nimap / nkmap, laid out as
+  // a B-column tile: column c of the tile is row c / 2, column c % 2 of the
   // box; the second column is past the spectrum: zeros in, not stored),
-  // after the full 16-column tiles, instead of one tile of 1 column per row
+  // after the full B-column tiles, instead of one tile of 1 column per row
   const int ntx = nyq_tiles > 0 ? ncols / B : (ncols + B - 1) / B;
   const long long nmain = (long long)ntx * ny;
   const long long ntiles = nmain + nyq_tiles;
@@ -742,7 +748,7 @@ static cudaError_t zconv_pipe_launch(float2* S, const float2* KXY, long long pit
     // lies past the spectrum)
     int nyq_tiles = 0;
     const int rem = ncols % P::B;
-    if (FC_ZNYQ && (FC_STORE_TMA & 2) && P::B == 16 && (rem == 1 || rem == 2) && ncols > P::B &&
+    if (FC_ZNYQ && (FC_STORE_TMA & 2) && P::B >= 4 && (rem == 1 || rem == 2) && ncols > P::B &&
         tile_tensor_map(&nimap, S, pitch, ny, ncols, N, 2, P::B / 2, P::ZBOX) &&
         tile_tensor_map(&nkmap, KXY, pitch, ny, ncols, kplanes, 2, P::B / 2, kbox))
       nyq_tiles = (ny + P::B / 2 - 1) / (P::B / 2);
