@@ -209,6 +209,7 @@ cudaError_t fast_cols_kx(const float2* kx_spec, long long pitch, int krows, int 
   return fast::dispatch_cols<false>(ax.n, s, dst, (long long)ax.n * pitch, pitch, ncols, nplanes, ax.W, st);
 }
 
+cudaError_t ycols_timeouts_addr(unsigned int** p) { return cudaGetSymbolAddress((void**)p, fast::g_ypipe_timeouts); }
 cudaError_t ycols_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
   return cudaMemcpyFromSymbolAsync(dst, fast::g_ypipe_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
 }

@@ -781,6 +781,9 @@ static cudaError_t zconv_pipe_launch(float2* S, const float2* KXY, long long pit
 static inline cudaError_t zstage_timeouts_read_async_tu(unsigned int* dst, cudaStream_t st) {
   return cudaMemcpyFromSymbolAsync(dst, g_zstage_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
 }
+static inline cudaError_t zstage_timeouts_addr_tu(unsigned int** p) {
+  return cudaGetSymbolAddress((void**)p, g_zstage_timeouts);
+}
 static inline void zstage_timeouts_clear_tu() {
   const unsigned int zero = 0;
   cudaMemcpyToSymbol(g_zstage_timeouts, &zero, sizeof(zero));

@@ -156,6 +156,8 @@ cudaError_t pipe_x_c2r(const float2* in, long long in_pitch, float* out, long lo
   }
 }
 
+cudaError_t pipe_timeouts_addr(unsigned int** p) { return cudaGetSymbolAddress((void**)p, fast::g_pipe_timeouts); }
+
 cudaError_t pipe_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
   return cudaMemcpyFromSymbolAsync(dst, fast::g_pipe_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
 }

@@ -52,6 +52,7 @@ cudaError_t fast_zconv_conj(float2* S, const float2* KXY, long long pitch, int n
   return fast::zconv_launch<true>(S, KXY, pitch, ny, ncols, kplanes, hz, scale, az, st);
 }
 
+cudaError_t zadj_timeouts_addr(unsigned int** p) { return fast::zstage_timeouts_addr_tu(p); }
 cudaError_t zadj_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
   return fast::zstage_timeouts_read_async_tu(dst, st);
 }

@@ -127,6 +127,7 @@ static cudaError_t zconv_launch(float2* S, const float2* KXY, long long pitch, i
 }
 }  // namespace fast
 
+cudaError_t zconv_timeouts_addr(unsigned int** p) { return fast::zstage_timeouts_addr_tu(p); }
 cudaError_t zconv_timeouts_read_async(unsigned int* dst, cudaStream_t st) {
   return fast::zstage_timeouts_read_async_tu(dst, st);
 }

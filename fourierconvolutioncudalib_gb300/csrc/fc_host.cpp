@@ -1072,8 +1072,28 @@ static bool host_buffer_pinned(const void* p) {
 // Bounded device waits (pipelined x passes, tensor-map stage of the fused z
 // passes): enqueue reads of their expiry counts on st, to be checked after
 // the stream's synchronisation by check_device_timeouts.
+// The six counts reach c.h_timeouts by one gather kernel writing the
+// page-locked buffer through its device address (instead of six small
+// device-to-host copies); the addresses are looked up on every call, so that
+// nothing stale survives a context that was torn down.  FC_GATHER_COUNTS=0
+// builds the copies, for comparison builds.
+#ifndef FC_GATHER_COUNTS
+#define FC_GATHER_COUNTS 1
+#endif
 static void enqueue_timeout_reads(DevCtx& c, cudaStream_t st) {
   if (!c.h_timeouts) host_alloc((void**)&c.h_timeouts, 8 * sizeof(unsigned int), "cudaHostAlloc(wait counts)");
+  if (FC_GATHER_COUNTS) {
+    unsigned int* src[6] = {};
+    unsigned int* dst = nullptr;
+    if (pipe_timeouts_addr(&src[0]) == cudaSuccess && zconv_timeouts_addr(&src[1]) == cudaSuccess &&
+        zadj_timeouts_addr(&src[2]) == cudaSuccess && tc_timeouts_addr_fp16(&src[3]) == cudaSuccess &&
+        tc_timeouts_addr_bf16(&src[4]) == cudaSuccess && ycols_timeouts_addr(&src[5]) == cudaSuccess &&
+        cudaHostGetDevicePointer((void**)&dst, c.h_timeouts, 0) == cudaSuccess) {
+      cuda_check(gather_counts_async(src, 6, dst, st), "timeout count gather");
+      return;
+    }
+    (void)cudaGetLastError();  // a failed lookup falls back to the copies
+  }
   cuda_check(pipe_timeouts_read_async(c.h_timeouts, st), "timeout count read");
   cuda_check(zconv_timeouts_read_async(c.h_timeouts + 1, st), "timeout count read");
   cuda_check(zadj_timeouts_read_async(c.h_timeouts + 2, st), "timeout count read");

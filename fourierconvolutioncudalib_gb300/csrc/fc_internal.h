@@ -123,6 +123,14 @@ cudaError_t pipe_x_c2r(const float2* in, long long in_pitch, float* out, long lo
                        const FcAxis& ax, cudaStream_t st);
 cudaError_t pipe_timeouts_read_async(unsigned int* dst, cudaStream_t st);
 void pipe_timeouts_clear();
+// the device address of each translation unit's count (current device), for
+// gather_counts_async
+cudaError_t pipe_timeouts_addr(unsigned int** p);
+cudaError_t zconv_timeouts_addr(unsigned int** p);
+cudaError_t zadj_timeouts_addr(unsigned int** p);
+cudaError_t ycols_timeouts_addr(unsigned int** p);
+// one kernel copies n counts (device addresses) to dst (device-visible memory)
+cudaError_t gather_counts_async(unsigned int* const* src, int n, unsigned int* dst, cudaStream_t st);
 // the same for the fused z passes' tensor-map stage copies (plain and
 // conjugate-kernel kernels)
 cudaError_t zconv_timeouts_read_async(unsigned int* dst, cudaStream_t st);
@@ -176,6 +184,7 @@ cudaError_t fast_zsub(float2* S, long long pitch, int ny, int ncols, const SubMa
   cudaError_t tc_zconv##sfx(float2* S, const float2* KXY, long long pitch, int ny, int ncols, int kplanes, int hz,  \
                             float scale, const FcAxis& az, cudaStream_t st);                                         \
   cudaError_t tc_timeouts_read_async##sfx(unsigned int* dst, cudaStream_t st);                                       \
+  cudaError_t tc_timeouts_addr##sfx(unsigned int** p);                                                               \
   void tc_timeouts_clear##sfx();
 FC_TC_DECL(_fp16)
 FC_TC_DECL(_bf16)

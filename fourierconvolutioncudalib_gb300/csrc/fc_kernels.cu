@@ -531,6 +531,27 @@ cudaError_t launch_crop_kernel(const float* vol, long long row_pitch, int ny_row
   return cudaGetLastError();
 }
 
+namespace {
+struct CountSrc {
+  unsigned int* p[8];
+  int n;
+};
+__global__ void k_gather_counts(CountSrc s, unsigned int* dst) {
+  const int i = (int)threadIdx.x;
+  if (i < s.n) dst[i] = *(volatile unsigned int*)s.p[i];
+  __threadfence_system();
+}
+}  // namespace
+
+cudaError_t gather_counts_async(unsigned int* const* src, int n, unsigned int* dst, cudaStream_t st) {
+  if (n < 1 || n > 8) return cudaErrorInvalidValue;
+  CountSrc s{};
+  for (int i = 0; i < n; ++i) s.p[i] = src[i];
+  s.n = n;
+  k_gather_counts<<<1, 32, 0, st>>>(s, dst);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_make_twiddles(float2* W, int n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   k_make_twiddles<<<(n + 255) / 256, 256, 0, st>>>(W, n);

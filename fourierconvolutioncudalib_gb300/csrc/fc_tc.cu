@@ -201,6 +201,9 @@ cudaError_t FC_TC_NAME(tc_zconv, FC_TC_SUFFIX)(float2* S, const float2* KXY, lon
   }
 }
 
+cudaError_t FC_TC_NAME(tc_timeouts_addr, FC_TC_SUFFIX)(unsigned int** p) {
+  return cudaGetSymbolAddress((void**)p, tc::g_tc5_timeouts);
+}
 cudaError_t FC_TC_NAME(tc_timeouts_read_async, FC_TC_SUFFIX)(unsigned int* dst, cudaStream_t st) {
   return cudaMemcpyFromSymbolAsync(dst, tc::g_tc5_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
 }
