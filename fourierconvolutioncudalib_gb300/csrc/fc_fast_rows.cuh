@@ -37,6 +37,9 @@ struct RowGeom {
 #endif
 template <int N, int TCM>
 constexpr bool kLineWarp = FC_ROW_WARPSYNC && TCM == tc::kNone && 32 % RowGeom<N>::T == 0;
+#ifndef FC_C2R_HALVES
+#define FC_C2R_HALVES 1
+#endif
 // the R2C pairs Z[k] with Z[N-k] by warp shuffles: a line of 32 threads (one
 // warp) whose last stage is radix 2 over 32 butterfly columns (N = 512);
 // FC_ROW_SHFL=0 builds the shared-memory pairing, for comparison builds
@@ -161,10 +164,37 @@ __device__ __forceinline__ void body_r2c(const Src& src, float2* __restrict__ ou
 template <int N, class In, bool REV = true>
 __device__ __forceinline__ void load_c2r(float2 (&v)[kVals], const In& in, const RowSlot<N>& s) {
   constexpr int R0 = first_radix<N, REV>();
+  constexpr int NB0 = N / R0, A0 = Plan<N>::A(R0);
 #pragma unroll
   for (int q = 0; q < kVals; ++q) {
     const int k = stage_pos<N, R0>(s.t, q);
     v[q] = make_float2(0.f, 0.f);
+    // position k = j + m N/R0 with j < N/R0: for an even R0 the half it lies in
+    // is known from m alone except at m = R0/2 (k = N/2 + j), so those values
+    // skip the runtime selection (FC_C2R_HALVES=0 builds the selection everywhere)
+    constexpr bool kHalves = FC_C2R_HALVES && R0 % 2 == 0 && N % 2 == 0;
+    const int m = q % R0;
+    if (kHalves && q < (kVals / R0) * R0 && 2 * m < R0) {
+      if (s.t < A0 && k >= 0) {  // low half: kk = k; the DC bin (m = 0, j = 0) is real
+        float2 a = s.va ? in.load(s.ra, k) : make_float2(0.f, 0.f);
+        float2 b = s.vb ? in.load(s.rb, k) : make_float2(0.f, 0.f);
+        if (m == 0 && k == 0) {
+          a.y = 0.f;
+          b.y = 0.f;
+        }
+        v[q] = make_float2(a.x - b.y, a.y + b.x);
+      }
+      continue;
+    }
+    if (kHalves && q < (kVals / R0) * R0 && 2 * m > R0) {
+      if (s.t < A0 && k >= 0) {  // high half: the conjugate of bin N - k (never DC or Nyquist)
+        const float2 a = s.va ? in.load(s.ra, N - k) : make_float2(0.f, 0.f);
+        const float2 b = s.vb ? in.load(s.rb, N - k) : make_float2(0.f, 0.f);
+        v[q] = make_float2(a.x + b.y, b.x - a.y);
+      }
+      continue;
+    }
+    (void)NB0;
     if (k >= 0) {
       const bool lo = k <= N / 2;
       const int kk = lo ? k : N - k;
